@@ -1,0 +1,178 @@
+/*
+ * umt103.h -- C-ABI of the GB300 (sm_103a) upstream-corner-balance sweep.
+ *
+ * This library replaces Teton's sweep/solve path below ControlSweep
+ * (src/teton/rt/ControlSweep.F90:15-81): the CPU SetSweep/SweepUCBxyz pair
+ * (snac/SetSweep.F90:10, snac/SweepUCBxyz.F90:11), the OpenMP-offload
+ * SetSweep_GPU (gpu/SetSweep_OMPOL.F90:12) and the CUDA gpu_sweepucbxyz
+ * (gpu/GPU_SweepUCBxyz.cu:532-572, bound from gpu/SweepUCBxyzToGPU.F90:44-90),
+ * plus the psi->phi tally getPhiTotal (control/getPhiTotal_OMPOL.F90:12) and
+ * the source-iteration loop of rtmainsn/LinearSolver
+ * (rt/rtmainsn.F90:167-246, rt/LinearSolver.F90:10-124).
+ *
+ * Conventions (all functions):
+ *   - return 0 on success, a negative UMT_ERR_* code otherwise; nothing
+ *     calls exit() or abort();
+ *   - called from one host thread; the library owns every device buffer;
+ *     host pointers are borrowed for the duration of the call only;
+ *   - index arrays are 0-based or 1-based per UmtMesh.index_base (Fortran
+ *     callers pass 1); the library converts once in umt103_init;
+ *   - arrays are in Teton's memory order: Psi(G,ncornr,A) is [a][c][g],
+ *     A_fp(3,maxcf,ncornr) is [c][cf][3], Sigt(G,nzones) is [z][g].
+ */
+#ifndef UMT103_H
+#define UMT103_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  UMT_OK = 0,
+  UMT_ERR_ARG = -1,        /* bad argument or size                         */
+  UMT_ERR_STATE = -2,      /* call order (e.g. sweep before init)          */
+  UMT_ERR_CUDA = -3,       /* CUDA runtime error                           */
+  UMT_ERR_CYCLE = -4,      /* mesh cycle the device schedule cannot order  */
+  UMT_ERR_TIMEOUT = -5,    /* a bounded device wait gave up                */
+  UMT_ERR_BOUNDS = -6,     /* device bounds check tripped                  */
+  UMT_ERR_NOMEM = -7,      /* device allocation failed                     */
+  UMT_ERR_NOTCONV = -8     /* iteration limit reached before convergence   */
+};
+
+/* precision of the angular-flux sweep */
+enum { UMT_FP64 = 0, UMT_FP32 = 1 };
+
+/*
+ * Mesh in Teton's corner representation: what teton_setzone
+ * (aux/setTetonZone.F90:10-202) stores in Geometry_mod.
+ */
+typedef struct UmtMesh {
+  int index_base;          /* 0 (C) or 1 (Fortran)                          */
+  int nzones, ncornr, nbelem;
+  int maxcf;               /* corner faces per corner, must be <= 3         */
+  int maxFaces;            /* row stride of zoneOpp/faceOpp, <= 6           */
+  const int *numCorner;    /* [nzones] corners per zone (<= 8)              */
+  const int *cOffSet;      /* [nzones] corners before this zone (a count)   */
+  const int *zoneFaces;    /* [nzones]                                      */
+  const int *zoneOpp;      /* [nzones*maxFaces] zone across face; < base => boundary */
+  const int *faceOpp;      /* [nzones*maxFaces] face index in that zone     */
+  const int *nCFaces;      /* [ncornr]                                      */
+  const int *cFP;          /* [ncornr*maxcf] corner across FP face, or ncornr+b */
+  const int *cEZ;          /* [ncornr*maxcf] zone-local corner across EZ face */
+  const int *CToFace;      /* [ncornr*maxcf] zone-local face of the corner face */
+  const int *bdyToC;       /* [nbelem] corner of each boundary element      */
+  const double *px;        /* [ncornr*3] vertex of each corner, or NULL     */
+  const double *A_fp;      /* [ncornr*maxcf*3] or NULL: computed on device  */
+  const double *A_ez;      /* [ncornr*maxcf*3] or NULL: computed on device  */
+  const double *Volume;    /* [ncornr] or NULL: computed on device          */
+} UmtMesh;
+
+/* Directions and weights (Quadrature_mod omega(3,A), weight(A)). */
+typedef struct UmtQuad {
+  int nangles;
+  const double *omega;     /* [nangles*3] */
+  const double *weight;    /* [nangles]   */
+} UmtQuad;
+
+/*
+ * umt103_init: upload mesh and quadrature, compute corner geometry on the
+ * device when not given (rt/geometryUCBxyz.F90:9-185) and build the sweep
+ * schedule of every direction on the device (replaces rtorder/snnext,
+ * rt/rtorder.F90:8-111, snac/snnext.F90:12-234, and findexit,
+ * rt/findexit.F90:296-347).  flags: bit0 = allocate the FP64 angular flux,
+ * bit1 = allocate the FP32 angular flux (both when 0).
+ */
+int umt103_init(const UmtMesh *mesh, const UmtQuad *quad, int ngr, int flags);
+
+/* Release every device buffer (idempotent). */
+void umt103_finalize(void);
+
+/*
+ * Materials: sigt = total opacity including tau, Sigt(G,nzones) as
+ * setTotalOpacity builds it (control/setTotalOpacity.F90:52); sigs =
+ * scattering opacity SigS(G,nzones) (may be NULL: no scattering); tau =
+ * 1/(c*dt) multiplying the previous-cycle angular flux in the source
+ * (snac/SweepUCBxyz.F90:121).
+ */
+int umt103_set_materials(const double *sigt, const double *sigs, double tau);
+
+/*
+ * Angular-flux state: Psi(G,ncornr,A) saved at the end of the last cycle
+ * (Set%Psi) and PsiB(G,nbelem,A) (Set%PsiB).  Either may be NULL (zero).
+ * Both precisions present are set from the FP64 input.
+ */
+int umt103_set_psi(const double *Psi, const double *PsiB);
+int umt103_get_psi(double *Psi, double *PsiB, int precision);
+
+/*
+ * One full sweep of every direction and group (SetSweep + getPhiTotal):
+ * source Q = STotal + tau*Psi; PhiTotal(G,ncornr) = sum_a w_a psi_a;
+ * exiting boundary fluxes written into PsiB; with savePsi the new angular
+ * flux becomes Psi.  STotal may be NULL (zero source, the mini-app case);
+ * PhiTotal_out and PsiB_inout may be NULL (results stay on the device).
+ */
+int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out,
+                 double *PsiB_inout, int precision);
+
+/*
+ * Device-resident variant for callers that keep everything in HBM: uses the
+ * source last set with umt103_set_source (or zero) and leaves PhiTotal on
+ * the device (read it with umt103_get_phi).
+ */
+int umt103_set_source(const double *STotal);
+int umt103_sweep_resident(int savePsi, int precision);
+int umt103_get_phi(double *PhiTotal);
+
+/* Source iteration (rtmainsn / LinearSolver / ConvergenceTest). */
+typedef struct UmtSIParams {
+  int precision;           /* UMT_FP64 or UMT_FP32                          */
+  int max_iters;           /* outer iterations (default 50)                 */
+  double rel_tol;          /* max relative change of zone phi               */
+  int use_gta;             /* 1: grey transport acceleration after each sweep */
+  const double *q_ext;     /* [nzones*G] isotropic external source, or NULL */
+  int save_psi;            /* final savePsi sweep                           */
+} UmtSIParams;
+
+typedef struct UmtSIResult {
+  int iterations;
+  int sweeps;
+  double rel_change;       /* last relative change of phi                   */
+  double seconds;          /* device time                                   */
+} UmtSIResult;
+
+int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);
+
+/*
+ * Energy tallies of the last sweep (rtedit, aux/rtedit.F90:8-327, and
+ * BoundaryEdit, control/BoundaryEdit.F90:9-215), accumulated in FP64.
+ */
+typedef struct UmtEnergyTally {
+  double EnergyRadiation;   /* sum V*PhiTotal / c                           */
+  double PowerEscape;       /* sum w (A_bdy.Omega>0) A_bdy.Omega psi         */
+  double PowerIncident;     /* sum w (A_bdy.Omega<0) |A_bdy.Omega| psiB      */
+  double PowerAbsorbed;     /* sum V sigma_a PhiTotal                        */
+  double Balance;           /* sweep balance residual (see DESIGN)          */
+} UmtEnergyTally;
+
+int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *tally);
+
+/* Schedule statistics for one direction. */
+int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);
+
+/* Copy out the device-built schedule: level of each (angle, zone) [A][nzones]
+ * and per-angle hyperplane counts. */
+int umt103_get_schedule(int *level, int *nHyperPlanes);
+
+/* Copy out the device geometry (A_fp, A_ez [ncornr*maxcf*3], Volume). */
+int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume);
+
+/* Device time of the last umt103_sweep* call in milliseconds, or < 0. */
+double umt103_last_sweep_ms(void);
+
+/* Last error text (static storage). */
+const char *umt103_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

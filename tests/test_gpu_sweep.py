@@ -1,0 +1,79 @@
+"""GPU parity: the CUDA sweep through the C-ABI against the CPU oracle."""
+import numpy as np
+import pytest
+
+from umt_gb300 import capi
+from umt_gb300.problems import uniform_problem, synthetic_problem
+from tests.helpers import oracle_sweep, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_gpu(lib, prob, precision, STotal=None, savePsi=True, Psi=None):
+    m = prob.mesh
+    lib.init(m, prob.omega, prob.weight, prob.ngr)
+    lib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    lib.set_psi(Psi if Psi is not None else prob.psi0, None)
+    A, G = len(prob.weight), prob.ngr
+    PsiB = np.zeros((A, m.nbelem, G))
+    Phi = lib.sweep(STotal, savePsi=savePsi, PsiB=PsiB, precision=precision)
+    Psi_out, _ = lib.get_psi(precision)
+    return Phi, Psi_out, PsiB
+
+
+def test_geometry_bitwise(umtlib):
+    prob = uniform_problem((2, 2, 2))
+    umtlib.init(prob.mesh, prob.omega, prob.weight, prob.ngr)
+    afp, aez, vol = umtlib.geometry()
+    ref = oracle_sweep(prob)["geo"]
+    assert np.array_equal(afp, ref[0])
+    assert np.array_equal(aez, ref[1])
+    assert np.array_equal(vol, ref[2])
+
+
+def test_schedule_levels_match_oracle_hyperplanes(umtlib):
+    prob = uniform_problem((3, 2, 2), 2, 2, 2)
+    umtlib.init(prob.mesh, prob.omega, prob.weight, prob.ngr)
+    level, nh = umtlib.schedule()
+    S = oracle_sweep(prob)["sched"]
+    for a in range(len(prob.weight)):
+        assert nh[a] == S.nHyperPlanes[a]
+        zl = np.zeros(prob.mesh.nzones, np.int32)
+        pos = 0
+        for h in range(S.nHyperPlanes[a]):
+            n = S.zonesInPlane[a, h]
+            zl[np.abs(S.nextZ[a, pos:pos + n])] = h
+            pos += n
+        assert np.array_equal(zl, level[a])
+
+
+@pytest.mark.parametrize("G", [2, 4, 16])
+def test_fp64_sweep_parity(umtlib, G):
+    prob = uniform_problem((2, 2, 2), 2, 2, G)
+    ref = oracle_sweep(prob, Psi=prob.psi0)
+    Phi, Psi, PsiB = _run_gpu(umtlib, prob, capi.UMT_FP64)
+    assert rel_err(Phi, ref["Phi"]) < 1e-12
+    assert rel_err(Psi, ref["Psi"]) < 1e-12
+    assert rel_err(PsiB, ref["PsiB"]) < 1e-12
+
+
+def test_fp64_sweep_parity_scattering_source(umtlib):
+    prob = synthetic_problem((2, 2, 1), 4, 4, 8, seed=7, time_dependent=True)
+    m = prob.mesh
+    rng = np.random.default_rng(1)
+    STotal = rng.uniform(0.1, 1.0, size=(m.ncornr, prob.ngr))
+    ref = oracle_sweep(prob, STotal=STotal, Psi=prob.psi0)
+    Phi, Psi, PsiB = _run_gpu(umtlib, prob, capi.UMT_FP64, STotal=STotal)
+    assert rel_err(Phi, ref["Phi"]) < 1e-12
+    assert rel_err(Psi, ref["Psi"]) < 1e-12
+
+
+def test_fp32_sweep_tolerance(umtlib):
+    prob = synthetic_problem((2, 2, 2), 2, 2, 16, seed=3, time_dependent=True)
+    m = prob.mesh
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    ref = oracle_sweep(prob, STotal=STotal, Psi=prob.psi0)
+    Phi, Psi, PsiB = _run_gpu(umtlib, prob, capi.UMT_FP32, STotal=STotal)
+    # FP32 sweep arithmetic: stated tolerance 1e-5 relative (max-norm) on phi
+    assert rel_err(Phi, ref["Phi"]) < 1e-5
+    assert rel_err(Psi, ref["Psi"]) < 1e-4

@@ -1,0 +1,197 @@
+"""ctypes binding of libumt103.so (include/umt103.h).
+
+This is the Python face of the C-ABI; a Fortran caller binds the same entry
+points through ISO_C_BINDING.  Loading fails loudly when
+the library has not been built: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libumt103.so")
+
+UMT_FP64, UMT_FP32 = 0, 1
+
+ERRORS = {0: "UMT_OK", -1: "UMT_ERR_ARG", -2: "UMT_ERR_STATE", -3: "UMT_ERR_CUDA",
+          -4: "UMT_ERR_CYCLE", -5: "UMT_ERR_TIMEOUT", -6: "UMT_ERR_BOUNDS",
+          -7: "UMT_ERR_NOMEM", -8: "UMT_ERR_NOTCONV"}
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+
+
+class UmtMesh(C.Structure):
+    _fields_ = [("index_base", C.c_int), ("nzones", C.c_int), ("ncornr", C.c_int),
+                ("nbelem", C.c_int), ("maxcf", C.c_int), ("maxFaces", C.c_int),
+                ("numCorner", _ip), ("cOffSet", _ip), ("zoneFaces", _ip), ("zoneOpp", _ip),
+                ("faceOpp", _ip), ("nCFaces", _ip), ("cFP", _ip), ("cEZ", _ip),
+                ("CToFace", _ip), ("bdyToC", _ip), ("px", _dp), ("A_fp", _dp),
+                ("A_ez", _dp), ("Volume", _dp)]
+
+
+class UmtQuad(C.Structure):
+    _fields_ = [("nangles", C.c_int), ("omega", _dp), ("weight", _dp)]
+
+
+class UmtSIParams(C.Structure):
+    _fields_ = [("precision", C.c_int), ("max_iters", C.c_int), ("rel_tol", C.c_double),
+                ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int)]
+
+
+class UmtSIResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("sweeps", C.c_int), ("rel_change", C.c_double),
+                ("seconds", C.c_double)]
+
+
+class UmtEnergyTally(C.Structure):
+    _fields_ = [("EnergyRadiation", C.c_double), ("PowerEscape", C.c_double),
+                ("PowerIncident", C.c_double), ("PowerAbsorbed", C.c_double),
+                ("Balance", C.c_double)]
+
+
+class UmtError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m umt_gb300.build` "
+                              "(the CUDA library is required, there is no CPU path)")
+        _lib = C.CDLL(LIB_PATH)
+        _lib.umt103_error_string.restype = C.c_char_p
+        _lib.umt103_last_sweep_ms.restype = C.c_double
+        _lib.umt103_finalize.restype = None
+        for n in ("umt103_init", "umt103_set_materials", "umt103_set_psi", "umt103_get_psi",
+                  "umt103_sweep", "umt103_set_source", "umt103_sweep_resident",
+                  "umt103_get_phi", "umt103_source_iterate", "umt103_tally",
+                  "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry"):
+            getattr(_lib, n).restype = C.c_int
+        _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
+        _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
+    return _lib
+
+
+EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_set_psi",
+            "umt103_get_psi", "umt103_sweep", "umt103_set_source", "umt103_sweep_resident",
+            "umt103_get_phi", "umt103_source_iterate", "umt103_tally", "umt103_schedule_info",
+            "umt103_get_schedule", "umt103_get_geometry", "umt103_last_sweep_ms",
+            "umt103_error_string"]
+
+
+def check(rc):
+    if rc != 0:
+        raise UmtError(rc, load().umt103_error_string().decode())
+    return rc
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _c(a, dt):
+    return None if a is None else np.ascontiguousarray(a, dtype=dt)
+
+
+class Library:
+    """Thin object wrapper keeping the argument arrays alive across calls."""
+
+    def __init__(self):
+        self.lib = load()
+        self._keep = []
+        self.A = self.G = self.nz = self.nc = self.nb = 0
+
+    def init(self, mesh, omega, weight, ngr, flags=0, with_geometry=None, index_base=0):
+        m = mesh
+        arrs = dict(numCorner=_c(m.numCorner, np.int32), cOffSet=_c(m.cOffSet, np.int32),
+                    zoneFaces=_c(m.zoneFaces, np.int32), zoneOpp=_c(m.zoneOpp, np.int32),
+                    faceOpp=_c(m.faceOpp, np.int32), nCFaces=_c(m.nCFaces, np.int32),
+                    cFP=_c(m.cFP, np.int32), cEZ=_c(m.cEZ, np.int32),
+                    CToFace=_c(m.CToFace, np.int32), bdyToC=_c(m.bdyToC, np.int32))
+        if index_base == 1:
+            for k in ("cFP", "cEZ", "CToFace", "bdyToC", "faceOpp"):
+                arrs[k] = arrs[k] + 1
+            zo = arrs["zoneOpp"].copy()
+            zo[zo >= 0] += 1
+            arrs["zoneOpp"] = zo
+            fo = arrs["faceOpp"].copy()
+            fo[arrs["zoneOpp"] < 1] = -1
+            arrs["faceOpp"] = fo
+        px = _c(m.px, np.float64)
+        geo = [None, None, None]
+        if with_geometry is not None:
+            geo = [_c(x, np.float64) for x in with_geometry]
+            px = None
+        st = UmtMesh(index_base, m.nzones, m.ncornr, m.nbelem, 3, m.zoneOpp.shape[1],
+                     _i(arrs["numCorner"]), _i(arrs["cOffSet"]), _i(arrs["zoneFaces"]),
+                     _i(arrs["zoneOpp"]), _i(arrs["faceOpp"]), _i(arrs["nCFaces"]),
+                     _i(arrs["cFP"]), _i(arrs["cEZ"]), _i(arrs["CToFace"]), _i(arrs["bdyToC"]),
+                     _d(px), _d(geo[0]), _d(geo[1]), _d(geo[2]))
+        om = _c(omega, np.float64); w = _c(weight, np.float64)
+        q = UmtQuad(len(w), _d(om), _d(w))
+        check(self.lib.umt103_init(C.byref(st), C.byref(q), int(ngr), int(flags)))
+        self.A, self.G, self.nz, self.nc, self.nb = len(w), int(ngr), m.nzones, m.ncornr, m.nbelem
+        return self
+
+    def finalize(self):
+        self.lib.umt103_finalize()
+
+    def set_materials(self, sigt, sigs=None, tau=0.0):
+        sigt = _c(sigt, np.float64); sigs = _c(sigs, np.float64)
+        check(self.lib.umt103_set_materials(_d(sigt), _d(sigs), C.c_double(tau)))
+
+    def set_psi(self, Psi=None, PsiB=None):
+        Psi = _c(Psi, np.float64); PsiB = _c(PsiB, np.float64)
+        check(self.lib.umt103_set_psi(_d(Psi), _d(PsiB)))
+
+    def get_psi(self, precision=UMT_FP64):
+        Psi = np.zeros((self.A, self.nc, self.G)); PsiB = np.zeros((self.A, self.nb, self.G))
+        check(self.lib.umt103_get_psi(_d(Psi), _d(PsiB), int(precision)))
+        return Psi, PsiB
+
+    def sweep(self, STotal=None, savePsi=False, PsiB=None, precision=UMT_FP64, want_phi=True):
+        STotal = _c(STotal, np.float64)
+        Phi = np.zeros((self.nc, self.G)) if want_phi else None
+        if PsiB is not None:
+            assert PsiB.dtype == np.float64 and PsiB.flags.c_contiguous
+        check(self.lib.umt103_sweep(_d(STotal), int(bool(savePsi)), _d(Phi), _d(PsiB), int(precision)))
+        return Phi
+
+    def set_source(self, STotal=None):
+        STotal = _c(STotal, np.float64)
+        check(self.lib.umt103_set_source(_d(STotal)))
+
+    def sweep_resident(self, savePsi=False, precision=UMT_FP64):
+        check(self.lib.umt103_sweep_resident(int(bool(savePsi)), int(precision)))
+
+    def get_phi(self):
+        Phi = np.zeros((self.nc, self.G))
+        check(self.lib.umt103_get_phi(_d(Phi)))
+        return Phi
+
+    def last_ms(self):
+        return float(self.lib.umt103_last_sweep_ms())
+
+    def schedule(self):
+        level = np.zeros((self.A, self.nz), np.int32); nh = np.zeros(self.A, np.int32)
+        check(self.lib.umt103_get_schedule(_i(level), _i(nh)))
+        return level, nh
+
+    def geometry(self):
+        afp = np.zeros((self.nc, 3, 3)); aez = np.zeros((self.nc, 3, 3)); vol = np.zeros(self.nc)
+        check(self.lib.umt103_get_geometry(_d(afp), _d(aez), _d(vol)))
+        return afp, aez, vol

@@ -1,0 +1,419 @@
+// capi.cu -- the extern "C" entry points declared in include/umt103.h.
+#include "umt_common.cuh"
+#include "../../include/umt103.h"
+
+#include <cstdarg>
+#include <cstring>
+#include <algorithm>
+
+namespace umt {
+
+Ctx g;
+std::string g_err;
+
+int set_error(int code, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+template <typename T>
+static int dalloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return set_error(UMT_ERR_NOMEM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+  }
+  return 0;
+}
+
+template <typename T>
+static void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+static void free_all() {
+  Ctx &c = g;
+  for (int i = 0; i < 2; ++i)
+    if (c.graph[i]) { cudaGraphExecDestroy(c.graph[i]); c.graph[i] = nullptr; }
+  dfree(c.numCorner); dfree(c.cOffSet); dfree(c.zoneFaces); dfree(c.zoneOpp); dfree(c.faceOpp);
+  dfree(c.nCFaces); dfree(c.cFP); dfree(c.cEZ); dfree(c.CToFace); dfree(c.bdyToC); dfree(c.cToZone);
+  dfree(c.px); dfree(c.A_fp); dfree(c.A_ez); dfree(c.Volume); dfree(c.VolumeZone); dfree(c.A_bdy);
+  dfree(c.Afp_raw); dfree(c.omega); dfree(c.weight);
+  dfree(c.afp64); dfree(c.aez64); dfree(c.afp32); dfree(c.aez32);
+  Schedule &s = c.sch;
+  dfree(s.items); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
+  dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
+  dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
+  for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
+  dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch);
+  if (c.ev0) cudaEventDestroy(c.ev0);
+  if (c.ev1) cudaEventDestroy(c.ev1);
+  if (c.stream) cudaStreamDestroy(c.stream);
+  c = Ctx();
+}
+
+static int upload_ints(int **dst, const int *src, size_t n, int shift) {
+  int rc = dalloc(dst, n);
+  if (rc) return rc;
+  std::vector<int> tmp(src, src + n);
+  if (shift)
+    for (auto &v : tmp) v -= shift;
+  UMT_CUDA(cudaMemcpy(*dst, tmp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+}  // namespace umt
+
+using namespace umt;
+
+#define TRY(x) do { int rc_ = (x); if (rc_) { return rc_; } } while (0)
+
+extern "C" {
+
+const char *umt103_error_string(void) { return g_err.c_str(); }
+
+void umt103_finalize(void) { free_all(); }
+
+int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
+  free_all();
+  if (!m || !q || ngr <= 0 || q->nangles <= 0 || !q->omega || !q->weight)
+    return set_error(UMT_ERR_ARG, "umt103_init: null mesh/quadrature or bad sizes");
+  if (m->maxcf > UMT_MAXCF || m->maxFaces > UMT_MAXFACES || m->maxcf <= 0)
+    return set_error(UMT_ERR_ARG, "umt103_init: maxcf must be <= %d and maxFaces <= %d", UMT_MAXCF, UMT_MAXFACES);
+  if (m->index_base != 0 && m->index_base != 1) return set_error(UMT_ERR_ARG, "index_base must be 0 or 1");
+  const int nz = m->nzones, nc = m->ncornr, nb = m->nbelem, A = q->nangles, G = ngr;
+  if (nz <= 0 || nc <= 0 || nb < 0) return set_error(UMT_ERR_ARG, "bad mesh sizes");
+  if ((size_t)A * nz >= (1ull << 31)) return set_error(UMT_ERR_ARG, "nangles*nzones must be < 2^31");
+  if (!m->px && !(m->A_fp && m->A_ez && m->Volume))
+    return set_error(UMT_ERR_ARG, "either px or A_fp/A_ez/Volume must be given");
+  const int base = m->index_base;
+  // host-side validation of sizes and index ranges
+  for (int z = 0; z < nz; ++z) {
+    if (m->numCorner[z] < 1 || m->numCorner[z] > UMT_MAXCORNER)
+      return set_error(UMT_ERR_ARG, "zone %d has %d corners (1..%d supported)", z, m->numCorner[z], UMT_MAXCORNER);
+    if (m->zoneFaces[z] < 1 || m->zoneFaces[z] > m->maxFaces)
+      return set_error(UMT_ERR_ARG, "zone %d has %d faces", z, m->zoneFaces[z]);
+    if (m->cOffSet[z] < 0 || m->cOffSet[z] + m->numCorner[z] > nc)
+      return set_error(UMT_ERR_ARG, "zone %d corner range out of bounds", z);
+  }
+  Ctx &c = g;
+  c.nz = nz; c.nc = nc; c.nb = nb; c.A = A; c.G = G; c.flags = flags ? flags : 3;
+  UMT_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  UMT_CUDA(cudaEventCreate(&c.ev0));
+  UMT_CUDA(cudaEventCreate(&c.ev1));
+  TRY(dalloc(&c.status, 1));
+  UMT_CUDA(cudaMemset(c.status, 0, sizeof(unsigned)));
+
+  // ---- mesh, converted to 0-based, padded to UMT_MAXCF / UMT_MAXFACES ----
+  const int mcf = m->maxcf, mf = m->maxFaces;
+  std::vector<int> cfp((size_t)nc * UMT_MAXCF, 0), cez((size_t)nc * UMT_MAXCF, 0), ctf((size_t)nc * UMT_MAXCF, 0);
+  std::vector<int> zo((size_t)nz * UMT_MAXFACES, -1), fo((size_t)nz * UMT_MAXFACES, -1);
+  std::vector<int> ncfv(m->nCFaces, m->nCFaces + nc);
+  std::vector<int> c2z(nc, -1);
+  for (int z = 0; z < nz; ++z)
+    for (int k = 0; k < m->numCorner[z]; ++k) c2z[m->cOffSet[z] + k] = z;
+  for (int cc = 0; cc < nc; ++cc) {
+    if (ncfv[cc] < 1 || ncfv[cc] > mcf) return set_error(UMT_ERR_ARG, "corner %d has %d corner faces", cc, ncfv[cc]);
+    const int z = c2z[cc];
+    if (z < 0) return set_error(UMT_ERR_ARG, "corner %d belongs to no zone", cc);
+    for (int k = 0; k < ncfv[cc]; ++k) {
+      const int vfp = m->cFP[(size_t)cc * mcf + k] - base;
+      const int vez = m->cEZ[(size_t)cc * mcf + k] - base;
+      const int vtf = m->CToFace[(size_t)cc * mcf + k] - base;
+      if (vfp < 0 || vfp >= nc + nb) return set_error(UMT_ERR_ARG, "cFP out of range at corner %d", cc);
+      if (vez < 0 || vez >= m->numCorner[z]) return set_error(UMT_ERR_ARG, "cEZ out of range at corner %d", cc);
+      if (vtf < 0 || vtf >= m->zoneFaces[z]) return set_error(UMT_ERR_ARG, "CToFace out of range at corner %d", cc);
+      cfp[(size_t)cc * UMT_MAXCF + k] = vfp;
+      cez[(size_t)cc * UMT_MAXCF + k] = vez;
+      ctf[(size_t)cc * UMT_MAXCF + k] = vtf;
+    }
+  }
+  for (int z = 0; z < nz; ++z)
+    for (int f = 0; f < m->zoneFaces[z]; ++f) {
+      const int v = m->zoneOpp[(size_t)z * mf + f];
+      const int zz = (v >= base) ? v - base : -1;
+      if (zz >= nz) return set_error(UMT_ERR_ARG, "zoneOpp out of range at zone %d", z);
+      zo[(size_t)z * UMT_MAXFACES + f] = zz;
+      fo[(size_t)z * UMT_MAXFACES + f] = zz >= 0 ? m->faceOpp[(size_t)z * mf + f] - base : -1;
+    }
+  std::vector<int> bdy(m->bdyToC, m->bdyToC + nb);
+  for (auto &v : bdy) { v -= base; if (v < 0 || v >= nc) return set_error(UMT_ERR_ARG, "bdyToC out of range"); }
+
+  TRY(upload_ints(&c.numCorner, m->numCorner, nz, 0));
+  TRY(upload_ints(&c.cOffSet, m->cOffSet, nz, 0));
+  TRY(upload_ints(&c.zoneFaces, m->zoneFaces, nz, 0));
+  TRY(upload_ints(&c.zoneOpp, zo.data(), zo.size(), 0));
+  TRY(upload_ints(&c.faceOpp, fo.data(), fo.size(), 0));
+  TRY(upload_ints(&c.nCFaces, ncfv.data(), nc, 0));
+  TRY(upload_ints(&c.cFP, cfp.data(), cfp.size(), 0));
+  TRY(upload_ints(&c.cEZ, cez.data(), cez.size(), 0));
+  TRY(upload_ints(&c.CToFace, ctf.data(), ctf.size(), 0));
+  TRY(upload_ints(&c.bdyToC, bdy.data(), nb, 0));
+  TRY(upload_ints(&c.cToZone, c2z.data(), nc, 0));
+
+  const size_t nA = (size_t)nc * UMT_MAXCF * 3;
+  TRY(dalloc(&c.A_fp, nA)); TRY(dalloc(&c.A_ez, nA)); TRY(dalloc(&c.Volume, nc));
+  TRY(dalloc(&c.VolumeZone, nz)); TRY(dalloc(&c.A_bdy, (size_t)nb * 3));
+  if (m->px) {
+    TRY(dalloc(&c.px, (size_t)nc * 3));
+    TRY(dalloc(&c.Afp_raw, nA));
+    UMT_CUDA(cudaMemcpy(c.px, m->px, (size_t)nc * 3 * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  if (m->A_fp && m->A_ez && m->Volume) {
+    std::vector<double> afp(nA, 0.0), aez(nA, 0.0);
+    for (int cc = 0; cc < nc; ++cc)
+      for (int k = 0; k < ncfv[cc]; ++k)
+        for (int d = 0; d < 3; ++d) {
+          afp[((size_t)cc * UMT_MAXCF + k) * 3 + d] = m->A_fp[((size_t)cc * mcf + k) * 3 + d];
+          aez[((size_t)cc * UMT_MAXCF + k) * 3 + d] = m->A_ez[((size_t)cc * mcf + k) * 3 + d];
+        }
+    UMT_CUDA(cudaMemcpy(c.A_fp, afp.data(), nA * sizeof(double), cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(c.A_ez, aez.data(), nA * sizeof(double), cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(c.Volume, m->Volume, nc * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<double> vz(nz, 0.0), ab((size_t)nb * 3, 0.0);
+    for (int z = 0; z < nz; ++z)
+      for (int k = 0; k < m->numCorner[z]; ++k) vz[z] += m->Volume[m->cOffSet[z] + k];
+    for (int cc = 0; cc < nc; ++cc)
+      for (int k = 0; k < ncfv[cc]; ++k) {
+        const int v = cfp[(size_t)cc * UMT_MAXCF + k];
+        if (v >= nc)
+          for (int d = 0; d < 3; ++d) ab[(size_t)(v - nc) * 3 + d] = afp[((size_t)cc * UMT_MAXCF + k) * 3 + d];
+      }
+    UMT_CUDA(cudaMemcpy(c.VolumeZone, vz.data(), nz * sizeof(double), cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(c.A_bdy, ab.data(), ab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  } else {
+    TRY(launch_geometry(c));
+  }
+
+  // ---- quadrature ----
+  c.h_omega.assign(q->omega, q->omega + 3 * (size_t)A);
+  c.h_weight.assign(q->weight, q->weight + A);
+  TRY(dalloc(&c.omega, 3 * (size_t)A)); TRY(dalloc(&c.weight, A));
+  UMT_CUDA(cudaMemcpy(c.omega, q->omega, 3 * (size_t)A * sizeof(double), cudaMemcpyHostToDevice));
+  UMT_CUDA(cudaMemcpy(c.weight, q->weight, (size_t)A * sizeof(double), cudaMemcpyHostToDevice));
+
+  // ---- projections (FP64 always: the schedule is decided in FP64) ----
+  const size_t nP = (size_t)A * nc * UMT_MAXCF;
+  TRY(dalloc(&c.afp64, nP)); TRY(dalloc(&c.aez64, nP));
+  if (c.flags & 2) { TRY(dalloc(&c.afp32, nP)); TRY(dalloc(&c.aez32, nP)); }
+  TRY(launch_projections(c));
+
+  // ---- schedule ----
+  Schedule &s = c.sch;
+  const size_t nAZ = (size_t)A * nz;
+  TRY(dalloc(&s.items, nAZ)); TRY(dalloc(&s.stageCount, nz + 2)); TRY(dalloc(&s.stageOffset, nz + 2));
+  TRY(dalloc(&s.need, nAZ)); TRY(dalloc(&s.exitMask, (nAZ + 3) & ~(size_t)3)); TRY(dalloc(&s.bad, nAZ));
+  TRY(dalloc(&s.order, nAZ)); TRY(dalloc(&s.level, nAZ)); TRY(dalloc(&s.nHyper, A));
+  TRY(dalloc(&s.processed, 1));
+  TRY(build_schedule(c));
+
+  // ---- state ----
+  const size_t ncG = (size_t)nc * G, nzG = (size_t)nz * G, psiN = (size_t)A * ncG, psiBN = (size_t)A * nb * G;
+  TRY(dalloc(&c.Sigt, nzG)); TRY(dalloc(&c.SigS, nzG));
+  TRY(dalloc(&c.STotal, ncG)); TRY(dalloc(&c.Phi, ncG));
+  UMT_CUDA(cudaMemset(c.Sigt, 0, nzG * sizeof(double)));
+  UMT_CUDA(cudaMemset(c.SigS, 0, nzG * sizeof(double)));
+  UMT_CUDA(cudaMemset(c.STotal, 0, ncG * sizeof(double)));
+  UMT_CUDA(cudaMemset(c.Phi, 0, ncG * sizeof(double)));
+  if (c.flags & 1) {
+    for (int i = 0; i < 2; ++i) { TRY(dalloc(&c.psi64[i], psiN)); UMT_CUDA(cudaMemset(c.psi64[i], 0, psiN * 8)); }
+    TRY(dalloc(&c.psiB64, psiBN)); UMT_CUDA(cudaMemset(c.psiB64, 0, psiBN * 8));
+  }
+  if (c.flags & 2) {
+    TRY(dalloc(&c.Sigt32, nzG)); TRY(dalloc(&c.STotal32, ncG));
+    for (int i = 0; i < 2; ++i) { TRY(dalloc(&c.psi32[i], psiN)); UMT_CUDA(cudaMemset(c.psi32[i], 0, psiN * 4)); }
+    TRY(dalloc(&c.psiB32, psiBN)); UMT_CUDA(cudaMemset(c.psiB32, 0, psiBN * 4));
+  }
+  UMT_CUDA(cudaDeviceSynchronize());
+  c.ready = true;
+  return 0;
+}
+
+int umt103_set_materials(const double *sigt, const double *sigs, double tau) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!sigt) return set_error(UMT_ERR_ARG, "sigt is required");
+  const size_t nzG = (size_t)c.nz * c.G;
+  for (size_t i = 0; i < nzG; ++i)
+    if (!(sigt[i] > 0.0)) return set_error(UMT_ERR_ARG, "sigt must be > 0 (element %zu)", i);
+  UMT_CUDA(cudaMemcpy(c.Sigt, sigt, nzG * 8, cudaMemcpyHostToDevice));
+  if (sigs) UMT_CUDA(cudaMemcpy(c.SigS, sigs, nzG * 8, cudaMemcpyHostToDevice));
+  else UMT_CUDA(cudaMemset(c.SigS, 0, nzG * 8));
+  c.tau = tau;
+  return 0;
+}
+
+__global__ void k_d2f(size_t n, const double *x, float *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+__global__ void k_f2d(size_t n, const float *x, double *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
+int umt103_set_psi(const double *Psi, const double *PsiB) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  const size_t psiN = (size_t)c.A * c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  double *tmp = nullptr;
+  TRY(dalloc(&tmp, std::max(psiN, psiBN)));
+  auto put = [&](const double *h, size_t n, double *d64, float *d32) -> int {
+    if (h) UMT_CUDA(cudaMemcpy(tmp, h, n * 8, cudaMemcpyHostToDevice));
+    else UMT_CUDA(cudaMemset(tmp, 0, n * 8));
+    if (d64) UMT_CUDA(cudaMemcpy(d64, tmp, n * 8, cudaMemcpyDeviceToDevice));
+    if (d32) k_d2f<<<4096, 256>>>(n, tmp, d32);
+    UMT_CUDA(cudaDeviceSynchronize());
+    return 0;
+  };
+  int rc = put(Psi, psiN, c.psi64[c.cur64], c.psi32[c.cur32]);
+  if (!rc) rc = put(PsiB, psiBN, c.psiB64, c.psiB32);
+  cudaFree(tmp);
+  return rc;
+}
+
+int umt103_get_psi(double *Psi, double *PsiB, int precision) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  const size_t psiN = (size_t)c.A * c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  if (precision == UMT_FP64) {
+    if (!c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
+    if (Psi) UMT_CUDA(cudaMemcpy(Psi, c.psi64[c.cur64], psiN * 8, cudaMemcpyDeviceToHost));
+    if (PsiB) UMT_CUDA(cudaMemcpy(PsiB, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost));
+    return 0;
+  }
+  if (!c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
+  double *tmp = nullptr;
+  TRY(dalloc(&tmp, std::max(psiN, psiBN)));
+  if (Psi) { k_f2d<<<4096, 256>>>(psiN, c.psi32[c.cur32], tmp); cudaMemcpy(Psi, tmp, psiN * 8, cudaMemcpyDeviceToHost); }
+  if (PsiB) { k_f2d<<<4096, 256>>>(psiBN, c.psiB32, tmp); cudaMemcpy(PsiB, tmp, psiBN * 8, cudaMemcpyDeviceToHost); }
+  cudaError_t e = cudaDeviceSynchronize();
+  cudaFree(tmp);
+  if (e != cudaSuccess) return set_error(UMT_ERR_CUDA, "get_psi: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+int umt103_set_source(const double *STotal) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  const size_t ncG = (size_t)c.nc * c.G;
+  if (STotal) UMT_CUDA(cudaMemcpy(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice));
+  else UMT_CUDA(cudaMemset(c.STotal, 0, ncG * 8));
+  return 0;
+}
+
+static int sweep_core(int savePsi, int precision) {
+  Ctx &c = g;
+  if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
+  if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
+  UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
+  TRY(launch_sweep_once(c, precision, true));
+  UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  cudaEventElapsedTime(&c.lastMs, c.ev0, c.ev1);
+  if (savePsi) {
+    if (precision == UMT_FP64) c.cur64 = 1 - c.cur64;
+    else c.cur32 = 1 - c.cur32;
+  }
+  unsigned st = 0;
+  UMT_CUDA(cudaMemcpy(&st, c.status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st & UMT_DEV_BOUNDS) return set_error(UMT_ERR_BOUNDS, "device bounds check");
+  if (st & UMT_DEV_TIMEOUT) return set_error(UMT_ERR_TIMEOUT, "device wait timed out");
+  return 0;
+}
+
+int umt103_sweep_resident(int savePsi, int precision) {
+  if (!g.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  return sweep_core(savePsi, precision);
+}
+
+int umt103_get_phi(double *PhiTotal) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  UMT_CUDA(cudaMemcpy(PhiTotal, c.Phi, (size_t)c.nc * c.G * 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double *PsiB_inout, int precision) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
+  else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
+  if (PsiB_inout) {
+    if (precision == UMT_FP64) {
+      UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
+    } else {
+      double *tmp = nullptr;
+      TRY(dalloc(&tmp, psiBN));
+      UMT_CUDA(cudaMemcpyAsync(tmp, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
+      k_d2f<<<4096, 256, 0, c.stream>>>(psiBN, tmp, c.psiB32);
+      UMT_CUDA(cudaStreamSynchronize(c.stream));
+      cudaFree(tmp);
+    }
+  }
+  TRY(sweep_core(savePsi, precision));
+  if (PhiTotal_out) UMT_CUDA(cudaMemcpy(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost));
+  if (PsiB_inout) {
+    if (precision == UMT_FP64) {
+      UMT_CUDA(cudaMemcpy(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost));
+    } else {
+      double *tmp = nullptr;
+      TRY(dalloc(&tmp, psiBN));
+      k_f2d<<<4096, 256, 0, c.stream>>>(psiBN, c.psiB32, tmp);
+      UMT_CUDA(cudaMemcpyAsync(PsiB_inout, tmp, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
+      UMT_CUDA(cudaStreamSynchronize(c.stream));
+      cudaFree(tmp);
+    }
+  }
+  return 0;
+}
+
+double umt103_last_sweep_ms(void) { return g.lastMs; }
+
+int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (angle < 0 || angle >= c.A) return set_error(UMT_ERR_ARG, "angle out of range");
+  int h = 0;
+  UMT_CUDA(cudaMemcpy(&h, c.sch.nHyper + angle, sizeof(int), cudaMemcpyDeviceToHost));
+  if (nHyperPlanes) *nHyperPlanes = h;
+  if (numCycles) *numCycles = 0;
+  return 0;
+}
+
+int umt103_get_schedule(int *level, int *nHyperPlanes) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (level) UMT_CUDA(cudaMemcpy(level, c.sch.level, (size_t)c.A * c.nz * sizeof(int), cudaMemcpyDeviceToHost));
+  if (nHyperPlanes) UMT_CUDA(cudaMemcpy(nHyperPlanes, c.sch.nHyper, c.A * sizeof(int), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  const size_t nA = (size_t)c.nc * UMT_MAXCF * 3;
+  if (A_fp) UMT_CUDA(cudaMemcpy(A_fp, c.A_fp, nA * 8, cudaMemcpyDeviceToHost));
+  if (A_ez) UMT_CUDA(cudaMemcpy(A_ez, c.A_ez, nA * 8, cudaMemcpyDeviceToHost));
+  if (Volume) UMT_CUDA(cudaMemcpy(Volume, c.Volume, (size_t)c.nc * 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int umt103_source_iterate(const UmtSIParams *, UmtSIResult *) {
+  return set_error(UMT_ERR_STATE, "source iteration not built yet");
+}
+
+int umt103_tally(const double *, double, UmtEnergyTally *) {
+  return set_error(UMT_ERR_STATE, "tally not built yet");
+}
+
+}  // extern "C"

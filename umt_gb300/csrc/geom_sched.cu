@@ -1,0 +1,390 @@
+// geom_sched.cu -- corner geometry and the device-built sweep schedule.
+//
+// Compiled with -fmad=false: the geometry and the signs of Omega.A that
+// decide upwind/downwind are computed with the same operation order as
+// Teton's Fortran (no contraction), so every dependency decision matches the
+// CPU schedule bit for bit and the sweep never reads a flux that its
+// schedule did not produce.
+#include "umt_common.cuh"
+
+namespace umt {
+
+// ---------------------------------------------------------------------------
+// Geometry: rt/geometryUCBxyz.F90:9-185 (area vectors of FP and EZ corner
+// faces, corner volumes) with the zone volume and boundary area vectors of
+// rt/volumeUCBxyz.F90.  One thread per zone.  Pass 1 computes each zone's own
+// FP area vectors and its EZ areas; pass 2 makes the FP vectors of shared
+// faces equal and opposite (the lower zone's vector wins, as in the
+// reference) and accumulates the volumes.
+// ---------------------------------------------------------------------------
+struct GeoArgs {
+  int nz, nc;
+  const int *numCorner, *cOffSet, *zoneFaces, *zoneOpp, *nCFaces, *cFP, *cEZ, *CToFace;
+  const double *px;
+  double *Afp_raw, *A_fp, *A_ez, *Volume, *VolumeZone, *A_bdy;
+};
+
+__device__ inline void zone_centres(const GeoArgs &p, int zone, double zc[3], double fc[UMT_MAXFACES][3]) {
+  const int nCorner = p.numCorner[zone], c0 = p.cOffSet[zone];
+  zc[0] = zc[1] = zc[2] = 0.0;
+  for (int c = 0; c < nCorner; ++c)
+    for (int d = 0; d < 3; ++d) zc[d] += p.px[3 * (c0 + c) + d];
+  for (int d = 0; d < 3; ++d) zc[d] /= (double)nCorner;
+  int ncf[UMT_MAXFACES];
+  for (int f = 0; f < UMT_MAXFACES; ++f) { ncf[f] = 0; fc[f][0] = fc[f][1] = fc[f][2] = 0.0; }
+  for (int c = 0; c < nCorner; ++c)
+    for (int cf = 0; cf < p.nCFaces[c0 + c]; ++cf) {
+      const int f = p.CToFace[(c0 + c) * UMT_MAXCF + cf];
+      ncf[f] += 1;
+      for (int d = 0; d < 3; ++d) fc[f][d] += p.px[3 * (c0 + c) + d];
+    }
+  for (int f = 0; f < UMT_MAXFACES; ++f)
+    for (int d = 0; d < 3; ++d) fc[f][d] = ncf[f] ? fc[f][d] / (double)ncf[f] : 0.0;
+}
+
+__global__ void k_geometry_pass1(GeoArgs p) {
+  const int zone = blockIdx.x * blockDim.x + threadIdx.x;
+  if (zone >= p.nz) return;
+  double zc[3], fc[UMT_MAXFACES][3];
+  zone_centres(p, zone, zc, fc);
+  const int nCorner = p.numCorner[zone], c0 = p.cOffSet[zone];
+  for (int c = 0; c < nCorner; ++c)
+    for (int k = 0; k < UMT_MAXCF * 3; ++k) p.A_ez[(size_t)(c0 + c) * UMT_MAXCF * 3 + k] = 0.0;
+  for (int c = 0; c < nCorner; ++c) {
+    const int cc = c0 + c, nCF = p.nCFaces[cc];
+    for (int cf1 = 0; cf1 < nCF; ++cf1) {
+      const int cf2 = (cf1 + 1) % nCF;
+      const int cez1 = p.cEZ[cc * UMT_MAXCF + cf1], cez2 = p.cEZ[cc * UMT_MAXCF + cf2];
+      const int face = p.CToFace[cc * UMT_MAXCF + cf1];
+      const double *p0 = p.px + 3 * cc, *p1 = p.px + 3 * (c0 + cez1), *p2 = p.px + 3 * (c0 + cez2);
+      double tdl[3], tfl[3], tfz[3], tfe1[3], tfe2[3];
+      for (int d = 0; d < 3; ++d) {
+        tdl[d] = 0.5 * (p1[d] - p2[d]);
+        tfl[d] = fc[face][d] - p0[d];
+        tfz[d] = fc[face][d] - zc[d];
+        tfe1[d] = fc[face][d] - 0.5 * (p1[d] + p0[d]);
+        tfe2[d] = fc[face][d] - 0.5 * (p2[d] + p0[d]);
+      }
+      double *raw = p.Afp_raw + ((size_t)cc * UMT_MAXCF + cf1) * 3;
+      raw[0] = 0.5 * (tfl[2] * tdl[1] - tfl[1] * tdl[2]);
+      raw[1] = 0.5 * (tfl[0] * tdl[2] - tfl[2] * tdl[0]);
+      raw[2] = 0.5 * (tfl[1] * tdl[0] - tfl[0] * tdl[1]);
+      double A1[3], A2[3];
+      A1[0] = 0.5 * (tfz[2] * tfe1[1] - tfz[1] * tfe1[2]);
+      A1[1] = 0.5 * (tfz[0] * tfe1[2] - tfz[2] * tfe1[0]);
+      A1[2] = 0.5 * (tfz[1] * tfe1[0] - tfz[0] * tfe1[1]);
+      A2[0] = 0.5 * (tfz[1] * tfe2[2] - tfz[2] * tfe2[1]);
+      A2[1] = 0.5 * (tfz[2] * tfe2[0] - tfz[0] * tfe2[2]);
+      A2[2] = 0.5 * (tfz[0] * tfe2[1] - tfz[1] * tfe2[0]);
+      for (int d = 0; d < 3; ++d) {
+        p.A_ez[((size_t)cc * UMT_MAXCF + cf1) * 3 + d] += A1[d];
+        p.A_ez[((size_t)cc * UMT_MAXCF + cf2) * 3 + d] += A2[d];
+      }
+    }
+  }
+  for (int c = 0; c < nCorner; ++c) {
+    const int cc = c0 + c;
+    for (int cf1 = 0; cf1 < p.nCFaces[cc]; ++cf1) {
+      const int cez = p.cEZ[cc * UMT_MAXCF + cf1];
+      if (cez > c)
+        for (int cf2 = 0; cf2 < p.nCFaces[c0 + cez]; ++cf2)
+          if (p.cEZ[(c0 + cez) * UMT_MAXCF + cf2] == c)
+            for (int d = 0; d < 3; ++d)
+              p.A_ez[((size_t)(c0 + cez) * UMT_MAXCF + cf2) * 3 + d] =
+                  -p.A_ez[((size_t)cc * UMT_MAXCF + cf1) * 3 + d];
+    }
+  }
+}
+
+__global__ void k_geometry_pass2(GeoArgs p) {
+  const int zone = blockIdx.x * blockDim.x + threadIdx.x;
+  if (zone >= p.nz) return;
+  double zc[3], fc[UMT_MAXFACES][3];
+  zone_centres(p, zone, zc, fc);
+  const int nCorner = p.numCorner[zone], c0 = p.cOffSet[zone];
+  double vz = 0.0;
+  for (int c = 0; c < nCorner; ++c) {
+    const int cc = c0 + c, nCF = p.nCFaces[cc];
+    double vol = 0.0;
+    for (int cf1 = 0; cf1 < nCF; ++cf1) {
+      const int face = p.CToFace[cc * UMT_MAXCF + cf1];
+      const int zOpp = p.zoneOpp[zone * UMT_MAXFACES + face];
+      const int cfp = p.cFP[cc * UMT_MAXCF + cf1];
+      double A[3];
+      const double *raw = p.Afp_raw + ((size_t)cc * UMT_MAXCF + cf1) * 3;
+      if (zOpp >= 0 && zOpp < zone) {
+        int cfo = -1;
+        for (int cf = 0; cf < p.nCFaces[cfp]; ++cf)
+          if (p.cFP[cfp * UMT_MAXCF + cf] == cc) cfo = cf;
+        const double *o = p.Afp_raw + ((size_t)cfp * UMT_MAXCF + (cfo < 0 ? 0 : cfo)) * 3;
+        for (int d = 0; d < 3; ++d) A[d] = -o[d];
+      } else {
+        for (int d = 0; d < 3; ++d) A[d] = raw[d];
+        if (zOpp < 0)
+          for (int d = 0; d < 3; ++d) p.A_bdy[3 * (size_t)(cfp - p.nc) + d] = raw[d];
+      }
+      for (int d = 0; d < 3; ++d) p.A_fp[((size_t)cc * UMT_MAXCF + cf1) * 3 + d] = A[d];
+      double tzl[3];
+      for (int d = 0; d < 3; ++d) tzl[d] = zc[d] - p.px[3 * cc + d];
+      vol += (1.0 / 3.0) * fabs(tzl[0] * A[0] + tzl[1] * A[1] + tzl[2] * A[2]);
+    }
+    p.Volume[cc] = vol;
+    vz += vol;
+  }
+  p.VolumeZone[zone] = vz;
+}
+
+int launch_geometry(Ctx &c) {
+  GeoArgs p{c.nz, c.nc, c.numCorner, c.cOffSet, c.zoneFaces, c.zoneOpp, c.nCFaces, c.cFP,
+            c.cEZ, c.CToFace, c.px, c.Afp_raw, c.A_fp, c.A_ez, c.Volume, c.VolumeZone, c.A_bdy};
+  const int T = 128, B = (c.nz + T - 1) / T;
+  k_geometry_pass1<<<B, T, 0, c.stream>>>(p);
+  k_geometry_pass2<<<B, T, 0, c.stream>>>(p);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-direction corner-face projections Omega.A_fp and Omega.A_ez (the
+// reference precomputes the same products as AfpNorm/AezNorm in
+// gpu/SweepUCBxyz_OMPOL.F90:141-252 and d_afp/d_aez in compAfpKernel,
+// gpu/GPU_SweepUCBxyz.cu:141-160).  FP64, summed in DOT_PRODUCT order.
+// ---------------------------------------------------------------------------
+__device__ inline double dot3(const double *o, const double *a) {
+  double s = 0.0;
+  s = s + o[0] * a[0];
+  s = s + o[1] * a[1];
+  s = s + o[2] * a[2];
+  return s;
+}
+
+__global__ void k_projections(int A, int nc, const double *omega, const int *nCFaces,
+                              const double *A_fp, const double *A_ez, double *afp64,
+                              double *aez64, float *afp32, float *aez32) {
+  const size_t n = (size_t)A * nc * UMT_MAXCF;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int cf = (int)(i % UMT_MAXCF);
+    const size_t ac = i / UMT_MAXCF;
+    const int c = (int)(ac % nc);
+    const int a = (int)(ac / nc);
+    double vf = 0.0, ve = 0.0;
+    if (cf < nCFaces[c]) {
+      const double *o = omega + 3 * a;
+      vf = dot3(o, A_fp + ((size_t)c * UMT_MAXCF + cf) * 3);
+      ve = dot3(o, A_ez + ((size_t)c * UMT_MAXCF + cf) * 3);
+    }
+    if (afp64) { afp64[i] = vf; aez64[i] = ve; }
+    if (afp32) { afp32[i] = (float)vf; aez32[i] = (float)ve; }
+  }
+}
+
+int launch_projections(Ctx &c) {
+  const size_t n = (size_t)c.A * c.nc * UMT_MAXCF;
+  int B = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  k_projections<<<B, 256, 0, c.stream>>>(c.A, c.nc, c.omega, c.nCFaces, c.A_fp, c.A_ez,
+                                         c.afp64, c.aez64, c.afp32, c.aez32);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Schedule.  k_need restates snneed (snac/snneed.F90:104-187): per zone face
+// the sum of Omega.A_fp over its corner faces decides the flow direction;
+// the downstream zone's need count is incremented and the upstream side's
+// face is marked as an exit.  A face whose corner faces disagree in sign
+// would need the reference's cycle list; it is reported as a cycle.
+// k_corner_order restates getDownStreamData (snac/getDownStreamData.F90:
+// 59-150): the corner solve order within a zone by repeated minloc of the
+// remaining EZ need; a zone whose corners cannot be ordered is "bad".
+// ---------------------------------------------------------------------------
+struct SchedArgs {
+  int nz, nc, A;
+  const int *numCorner, *cOffSet, *zoneFaces, *zoneOpp, *faceOpp, *nCFaces, *cEZ, *CToFace;
+  const double *afp64, *aez64;
+  int *need;
+  uint8_t *exitMask, *bad;
+  uint32_t *order;
+  unsigned int *status;
+};
+
+__global__ void k_need(SchedArgs p) {
+  const size_t n = (size_t)p.A * p.nz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int zone = (int)(i % p.nz), a = (int)(i / p.nz);
+    const int nCorner = p.numCorner[zone], c0 = p.cOffSet[zone];
+    double afpm_Face[UMT_MAXFACES];
+    int nInc[UMT_MAXFACES], nExit[UMT_MAXFACES];
+    for (int f = 0; f < UMT_MAXFACES; ++f) { afpm_Face[f] = 0.0; nInc[f] = 0; nExit[f] = 0; }
+    for (int c = 0; c < nCorner; ++c) {
+      const int cc = c0 + c;
+      for (int cf = 0; cf < p.nCFaces[cc]; ++cf) {
+        const int face = p.CToFace[cc * UMT_MAXCF + cf];
+        if (p.zoneOpp[zone * UMT_MAXFACES + face] > zone) {
+          const double afpm = p.afp64[((size_t)a * p.nc + cc) * UMT_MAXCF + cf];
+          afpm_Face[face] = afpm_Face[face] + afpm;
+          if (afpm < 0.0) nInc[face] += 1;
+          else if (afpm > 0.0) nExit[face] += 1;
+        }
+      }
+    }
+    for (int face = 0; face < p.zoneFaces[zone]; ++face) {
+      const int zOpp = p.zoneOpp[zone * UMT_MAXFACES + face];
+      if (zOpp > zone) {
+        const int fOpp = p.faceOpp[zone * UMT_MAXFACES + face];
+        if (afpm_Face[face] < 0.0) {
+          atomicAdd(&p.need[(size_t)a * p.nz + zone], 1);
+          atomicOr((unsigned int *)(p.exitMask + (((size_t)a * p.nz + zOpp) & ~(size_t)3)),
+                   (1u << fOpp) << (8 * (((size_t)a * p.nz + zOpp) & 3)));
+          if (nExit[face] > 0) atomicOr(p.status, UMT_DEV_CYCLE);
+        } else if (afpm_Face[face] > 0.0) {
+          atomicAdd(&p.need[(size_t)a * p.nz + zOpp], 1);
+          atomicOr((unsigned int *)(p.exitMask + (i & ~(size_t)3)), (1u << face) << (8 * (i & 3)));
+          if (nInc[face] > 0) atomicOr(p.status, UMT_DEV_CYCLE);
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_corner_order(SchedArgs p) {
+  const size_t n = (size_t)p.A * p.nz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int zone = (int)(i % p.nz), a = (int)(i / p.nz);
+    const int nCorner = p.numCorner[zone], c0 = p.cOffSet[zone];
+    int need[UMT_MAXCORNER], nDSC[UMT_MAXCORNER];
+    int DSC[UMT_MAXCORNER][UMT_MAXCORNER];
+    for (int c = 0; c < UMT_MAXCORNER; ++c) { need[c] = 0; nDSC[c] = 0; }
+    for (int c = 0; c < nCorner; ++c) {
+      const int cc = c0 + c;
+      for (int cf = 0; cf < p.nCFaces[cc]; ++cf) {
+        const int cez = p.cEZ[cc * UMT_MAXCF + cf];
+        if (cez > c) {
+          const double aez = p.aez64[((size_t)a * p.nc + cc) * UMT_MAXCF + cf];
+          if (aez < 0.0) { need[c] += 1; DSC[cez][nDSC[cez]++] = c; }
+          else if (aez > 0.0) { need[cez] += 1; DSC[c][nDSC[c]++] = cez; }
+        }
+      }
+    }
+    bool isbad = false;
+    uint32_t ord = 0;
+    for (int k = 0; k < nCorner; ++k) {
+      int c = 0;
+      for (int m = 1; m < nCorner; ++m) if (need[m] < need[c]) c = m;
+      ord |= (uint32_t)c << (4 * k);
+      if (need[c] != 0) isbad = true;
+      for (int m = 0; m < nDSC[c]; ++m) need[DSC[c][m]] -= 1;
+      need[c] = 99;
+    }
+    if (isbad) {
+      ord = 0;
+      for (int k = 0; k < nCorner; ++k) ord |= (uint32_t)k << (4 * k);
+      atomicOr(p.status, UMT_DEV_CYCLE);
+    }
+    p.order[i] = ord;
+    p.bad[i] = isbad ? 1 : 0;
+  }
+}
+
+// Stage 0: every (direction, zone) that needs no upwind zone (findseeds,
+// snac/findseeds.F90:58-65).
+__global__ void k_seed(int nz, int A, const int *need, const uint8_t *bad, uint32_t *items,
+                       int *stageCount, int *level, unsigned long long *processed) {
+  const size_t n = (size_t)A * nz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (need[i] == 0) {
+      const int pos = atomicAdd(&stageCount[0], 1);
+      items[pos] = (uint32_t)i | (bad[i] ? 0x80000000u : 0u);
+      level[i] = 0;
+    }
+  }
+}
+
+// Stage h -> h+1 (the hyperplane loop of snac/snnext.F90:109-163): every item
+// of stage h decrements the need of its downstream zones; a zone whose need
+// reaches zero joins stage h+1.  Items of one stage are independent.
+__global__ void k_stage(int h, int nz, int A, const int *zoneFaces, const int *zoneOpp,
+                        const uint8_t *exitMask, const uint8_t *bad, int *need, uint32_t *items,
+                        int *stageCount, int *stageOffset, int *level, int *nHyper,
+                        unsigned long long *processed) {
+  const int off = stageOffset[h], cnt = stageCount[h];
+  const int offn = off + cnt;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    stageOffset[h + 1] = offn;
+    if (cnt) atomicAdd(processed, (unsigned long long)cnt);
+  }
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const uint32_t it = items[off + k] & 0x7fffffffu;
+    const int a = (int)(it / (uint32_t)nz), z = (int)(it - (uint32_t)a * nz);
+    atomicMax(&nHyper[a], h + 1);
+    const uint8_t m = exitMask[it];
+    for (int f = 0; f < zoneFaces[z]; ++f) {
+      if (m & (1u << f)) {
+        const int zo = zoneOpp[z * UMT_MAXFACES + f];
+        if (zo >= 0) {
+          const size_t j = (size_t)a * nz + zo;
+          if (atomicSub(&need[j], 1) == 1) {
+            const int pos = atomicAdd(&stageCount[h + 1], 1);
+            items[offn + pos] = (uint32_t)j | (bad[j] ? 0x80000000u : 0u);
+            level[j] = h + 1;
+          }
+        }
+      }
+    }
+  }
+}
+
+int build_schedule(Ctx &c) {
+  Schedule &s = c.sch;
+  const size_t n = (size_t)c.A * c.nz;
+  UMT_CUDA(cudaMemsetAsync(s.need, 0, n * sizeof(int), c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.exitMask, 0, ((n + 3) & ~(size_t)3), c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.stageCount, 0, (c.nz + 2) * sizeof(int), c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.stageOffset, 0, (c.nz + 2) * sizeof(int), c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.nHyper, 0, c.A * sizeof(int), c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.processed, 0, sizeof(unsigned long long), c.stream));
+  SchedArgs p{c.nz, c.nc, c.A, c.numCorner, c.cOffSet, c.zoneFaces, c.zoneOpp, c.faceOpp,
+              c.nCFaces, c.cEZ, c.CToFace, c.afp64, c.aez64, s.need, s.exitMask, s.bad, s.order, c.status};
+  const int B = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+  k_need<<<B, 256, 0, c.stream>>>(p);
+  k_corner_order<<<B, 256, 0, c.stream>>>(p);
+  k_seed<<<B, 256, 0, c.stream>>>(c.nz, c.A, s.need, s.bad, s.items, s.stageCount, s.level, s.processed);
+  UMT_CUDA(cudaGetLastError());
+  unsigned int st = 0;
+  UMT_CUDA(cudaMemcpyAsync(&st, c.status, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  if (st & UMT_DEV_CYCLE)
+    return set_error(-4, "mesh has a zone face or zone corner cycle for some direction; "
+                         "lagged (cycle-list) sweeps are not supported by the device schedule");
+  // stages: launch in batches, stop when every item is placed
+  int h = 0;
+  const int batch = 32;
+  const int SB = 152 * 8;
+  unsigned long long placed = 0;
+  int lastCount = -1;
+  while (true) {
+    for (int k = 0; k < batch && h < c.nz; ++k, ++h)
+      k_stage<<<SB, 256, 0, c.stream>>>(h, c.nz, c.A, c.zoneFaces, c.zoneOpp, s.exitMask, s.bad, s.need,
+                                        s.items, s.stageCount, s.stageOffset, s.level, s.nHyper, s.processed);
+    UMT_CUDA(cudaGetLastError());
+    UMT_CUDA(cudaMemcpyAsync(&placed, s.processed, sizeof(placed), cudaMemcpyDeviceToHost, c.stream));
+    UMT_CUDA(cudaMemcpyAsync(&lastCount, s.stageCount + h, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    UMT_CUDA(cudaStreamSynchronize(c.stream));
+    if (placed == n) break;
+    if (lastCount == 0 || h >= c.nz)
+      return set_error(-4, "schedule stalled after %d stages (%llu of %zu items): mesh cycle", h, placed, n);
+  }
+  s.hCount.assign(c.nz + 2, 0);
+  s.hOffset.assign(c.nz + 2, 0);
+  UMT_CUDA(cudaMemcpy(s.hCount.data(), s.stageCount, (c.nz + 2) * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(s.hOffset.data(), s.stageOffset, (c.nz + 2) * sizeof(int), cudaMemcpyDeviceToHost));
+  s.nStages = 0;
+  s.maxStageItems = 0;
+  for (int k = 0; k < c.nz + 1; ++k) {
+    if (s.hCount[k] == 0) break;
+    s.nStages = k + 1;
+    s.maxStageItems = std::max(s.maxStageItems, s.hCount[k]);
+  }
+  return 0;
+}
+
+}  // namespace umt

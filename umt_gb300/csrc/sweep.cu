@@ -1,0 +1,270 @@
+// sweep.cu -- the upstream-corner-balance sweep, the psi->phi tally and the
+// source/energy helpers.
+//
+// Work decomposition: the schedule orders every (direction, zone) pair into
+// dependency stages; one kernel per stage processes all pairs of the stage,
+// for every direction at once.  A team of GT consecutive lanes owns one
+// (direction, zone) pair and walks its groups g = lane, lane+GT, ...; the
+// zone's corner-face data (Omega.A, neighbour corners, volumes) is staged
+// once per team in shared memory and read by all lanes.  Psi is stored
+// group-innermost, [direction][corner][group], so a team's loads and stores
+// of one corner are one contiguous segment.  The per-stage launches of a
+// whole sweep, plus the tally, are captured once into a CUDA graph.
+//
+// Arithmetic per (corner, group) restates snac/SweepUCBxyz.F90:103-312 in the
+// same operation order (FP64 instantiation is the parity path; the FP32
+// instantiation is the production path).
+#include "umt_common.cuh"
+
+namespace umt {
+
+template <typename T>
+struct SweepP {
+  int nz, nc, nb, A, G;
+  const uint32_t *items;
+  const int *stageOffset, *stageCount;
+  const uint32_t *order;
+  const int *numCorner, *cOffSet, *nCFaces, *cFP, *cEZ;
+  const T *afp, *aez;
+  const double *Volume;
+  const T *Sigt, *STotal;
+  T tau;
+  const T *psi_old;
+  T *psi_new, *psiB;
+};
+
+constexpr int SWEEP_NT = 128;
+
+template <typename T, int GT>
+__global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
+  constexpr int TEAMS = SWEEP_NT / GT;
+  __shared__ T s_src[UMT_MAXCORNER][SWEEP_NT];
+  __shared__ T s_Q[UMT_MAXCORNER][SWEEP_NT];
+  __shared__ T s_psi[UMT_MAXCORNER][SWEEP_NT];
+  __shared__ T s_afp[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
+  __shared__ T s_aez[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
+  __shared__ T s_sum[TEAMS][UMT_MAXCORNER];
+  __shared__ T s_vol[TEAMS][UMT_MAXCORNER];
+  __shared__ int s_cfp[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
+  __shared__ int8_t s_cez[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
+  __shared__ int8_t s_ncf[TEAMS][UMT_MAXCORNER];
+
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const int k = blockIdx.x * TEAMS + team;
+  const int cnt = p.stageCount[stage];
+  if (k >= cnt) return;                       // whole teams leave together
+  const unsigned teammask = (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
+  uint32_t it = p.items[p.stageOffset[stage] + k];
+  const bool bad = (it >> 31) != 0;
+  it &= 0x7fffffffu;
+  const int a = (int)(it / (uint32_t)p.nz);
+  const int z = (int)(it - (uint32_t)a * p.nz);
+  const int nCorner = p.numCorner[z], c0 = p.cOffSet[z];
+  const uint32_t ord = p.order[it];
+  const size_t abase = (size_t)a * p.nc;
+
+  for (int c = lane; c < nCorner; c += GT) {
+    const int cc = c0 + c;
+    const int ncf = p.nCFaces[cc];
+    s_ncf[team][c] = (int8_t)ncf;
+    s_vol[team][c] = (T)p.Volume[cc];
+    T sum = T(0);
+#pragma unroll
+    for (int cf = 0; cf < UMT_MAXCF; ++cf) {
+      const T v = p.afp[(abase + cc) * UMT_MAXCF + cf];
+      s_afp[team][c][cf] = v;
+      s_cfp[team][c][cf] = p.cFP[cc * UMT_MAXCF + cf];
+      if (cf < ncf && v > T(0)) sum = sum + v;
+    }
+#pragma unroll
+    for (int cf = 0; cf < UMT_MAXCF; ++cf) {
+      const T v = p.aez[(abase + cc) * UMT_MAXCF + cf];
+      s_aez[team][c][cf] = v;
+      s_cez[team][c][cf] = (int8_t)p.cEZ[cc * UMT_MAXCF + cf];
+      if (cf < ncf && v > T(0)) sum = sum + v;
+    }
+    s_sum[team][c] = sum;
+  }
+  __syncwarp(teammask);
+
+  const T fouralpha = T(1.82);
+  const T *sigz = p.Sigt + (size_t)z * p.G;
+  for (int g = lane; g < p.G; g += GT) {
+    const T sig = sigz[g];
+    for (int c = 0; c < nCorner; ++c) {
+      const size_t e = (size_t)(c0 + c) * p.G + g;
+      const T st = p.STotal ? p.STotal[e] : T(0);
+      const T q = st + p.tau * p.psi_old[abase * p.G + e];
+      s_Q[c][tid] = q;
+      s_src[c][tid] = s_vol[team][c] * q;
+    }
+    for (int c = 0; c < nCorner; ++c) {
+      const int ncf = s_ncf[team][c];
+      T psifp[UMT_MAXCF];
+      T srcc = s_src[c][tid];
+#pragma unroll
+      for (int cf = 0; cf < UMT_MAXCF; ++cf) {
+        psifp[cf] = T(0);
+        const T af = s_afp[team][c][cf];
+        if (cf < ncf && af < T(0)) {
+          const int cfp = s_cfp[team][c][cf];
+          const T pu = (cfp < p.nc) ? p.psi_new[(abase + cfp) * p.G + g]
+                                    : p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g];
+          psifp[cf] = pu;
+          srcc = srcc - af * pu;
+        }
+      }
+      s_src[c][tid] = srcc;
+      const T Qc = s_Q[c][tid];
+#pragma unroll
+      for (int cf = 0; cf < UMT_MAXCF; ++cf) {
+        const T aez = s_aez[team][c][cf];
+        if (cf < ncf && aez > T(0)) {
+          const int cez = s_cez[team][c][cf];
+          T area_opp = T(0), psi_opp = T(0);
+          if (ncf == 3) {
+            const int ifp = (cf + 1) % 3;
+            const T afo = s_afp[team][c][ifp];
+            if (afo < T(0)) { psi_opp = psifp[ifp]; area_opp = -afo; }
+          }
+          const T Qz = s_Q[cez][tid];
+          T sez;
+          if (area_opp > T(0)) {
+            const T aez2 = aez * aez;
+            const T vol = s_vol[team][c];
+            const T sigv = sig * vol;
+            const T sigv2 = sigv * sigv;
+            const T gnum = aez2 * (fouralpha * sigv2 + aez * (T(4) * sigv + T(3) * aez));
+            const T gden = vol * (T(4) * sigv * sigv2 + aez * (T(6) * sigv2 + T(2) * aez * (T(2) * sigv + aez)));
+            sez = (vol * gnum * (sig * psi_opp - Qc) + T(0.5) * aez * gden * (Qc - Qz)) / (gnum + gden * sig);
+          } else {
+            const T sigInv = T(1) / sig;
+            sez = T(0.5) * aez * sigInv * (Qc - Qz);
+          }
+          s_src[c][tid] = s_src[c][tid] + sez;
+          s_src[cez][tid] = s_src[cez][tid] - sez;
+        }
+      }
+    }
+    T *out = p.psi_new + abase * p.G;
+    if (!bad) {
+      for (int i = 0; i < nCorner; ++i) {
+        const int c = (int)((ord >> (4 * i)) & 15u);
+        const T v = s_src[c][tid] / (s_sum[team][c] + sig * s_vol[team][c]);
+        out[(size_t)(c0 + c) * p.G + g] = v;
+        s_psi[c][tid] = v;
+        const int ncf = s_ncf[team][c];
+#pragma unroll
+        for (int cf = 0; cf < UMT_MAXCF; ++cf) {
+          const T aez = s_aez[team][c][cf];
+          if (cf < ncf && aez > T(0)) {
+            const int cez = s_cez[team][c][cf];
+            s_src[cez][tid] = s_src[cez][tid] + aez * v;
+          }
+        }
+      }
+    } else {
+      // direct solve with the previous iterate of this zone (SweepUCBxyz.F90:283-297)
+      for (int c = 0; c < nCorner; ++c) {
+        const T old = out[(size_t)(c0 + c) * p.G + g];
+        const int ncf = s_ncf[team][c];
+        for (int cf = 0; cf < ncf; ++cf) {
+          const T aez = s_aez[team][c][cf];
+          if (aez > T(0)) {
+            const int cez = s_cez[team][c][cf];
+            s_src[cez][tid] = s_src[cez][tid] + aez * old;
+          }
+        }
+      }
+      for (int c = 0; c < nCorner; ++c) {
+        const T v = s_src[c][tid] / (s_sum[team][c] + sig * s_vol[team][c]);
+        out[(size_t)(c0 + c) * p.G + g] = v;
+        s_psi[c][tid] = v;
+      }
+    }
+    // exiting boundary fluxes
+    for (int c = 0; c < nCorner; ++c) {
+      const int ncf = s_ncf[team][c];
+      for (int cf = 0; cf < ncf; ++cf) {
+        const int cfp = s_cfp[team][c][cf];
+        if (cfp >= p.nc && s_afp[team][c][cf] > T(0))
+          p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g] = s_psi[c][tid];
+      }
+    }
+  }
+}
+
+// psi -> phi tally: PhiTotal(g,c) = sum_a w_a psi_a(g,c), accumulated in FP64
+// (control/getPhiTotal_OMPOL.F90:63-131 does the same per direction).
+template <typename T>
+__global__ void k_tally(int A, size_t ncG, const double *weight, const T *psi, double *Phi) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncG; e += (size_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int a = 0; a < A; ++a) s += weight[a] * (double)psi[(size_t)a * ncG + e];
+    Phi[e] = s;
+  }
+}
+
+__global__ void k_to_float(size_t n, const double *x, float *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+template <typename T>
+static int enqueue_sweep(Ctx &c, int cur) {
+  SweepP<T> p;
+  p.nz = c.nz; p.nc = c.nc; p.nb = c.nb; p.A = c.A; p.G = c.G;
+  p.items = c.sch.items; p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
+  p.order = c.sch.order;
+  p.numCorner = c.numCorner; p.cOffSet = c.cOffSet; p.nCFaces = c.nCFaces; p.cFP = c.cFP; p.cEZ = c.cEZ;
+  p.Volume = c.Volume;
+  p.tau = (T)c.tau;
+  if constexpr (sizeof(T) == 8) {
+    p.afp = (const T *)c.afp64; p.aez = (const T *)c.aez64;
+    p.Sigt = (const T *)c.Sigt; p.STotal = (const T *)c.STotal;
+    p.psi_old = (const T *)c.psi64[cur]; p.psi_new = (T *)c.psi64[1 - cur]; p.psiB = (T *)c.psiB64;
+  } else {
+    p.afp = (const T *)c.afp32; p.aez = (const T *)c.aez32;
+    p.Sigt = (const T *)c.Sigt32; p.STotal = (const T *)c.STotal32;
+    p.psi_old = (const T *)c.psi32[cur]; p.psi_new = (T *)c.psi32[1 - cur]; p.psiB = (T *)c.psiB32;
+  }
+  const int prec = sizeof(T) == 8 ? 0 : 1;
+  int GT = c.sweepGT[prec];
+  if (GT <= 0) {
+    GT = 1;
+    while (GT < c.G && GT < 32) GT *= 2;
+    c.sweepGT[prec] = GT;
+  }
+  const int TEAMS = SWEEP_NT / GT;
+  if constexpr (sizeof(T) == 4) {
+    const size_t n = (size_t)c.nz * c.G;
+    k_to_float<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(n, c.Sigt, c.Sigt32);
+    const size_t m = (size_t)c.nc * c.G;
+    k_to_float<<<(int)std::min<size_t>((m + 255) / 256, 4096), 256, 0, c.stream>>>(m, c.STotal, c.STotal32);
+  }
+  for (int s = 0; s < c.sch.nStages; ++s) {
+    const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;
+    switch (GT) {
+      case 1: k_sweep<T, 1><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
+      case 2: k_sweep<T, 2><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
+      case 4: k_sweep<T, 4><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
+      case 8: k_sweep<T, 8><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
+      case 16: k_sweep<T, 16><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
+      default: k_sweep<T, 32><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
+    }
+  }
+  const size_t ncG = (size_t)c.nc * c.G;
+  k_tally<T><<<(int)std::min<size_t>((ncG + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
+      c.A, ncG, c.weight, (const T *)(sizeof(T) == 8 ? (const void *)c.psi64[1 - cur] : (const void *)c.psi32[1 - cur]), c.Phi);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int launch_sweep_once(Ctx &c, int precision, bool /*tally*/) {
+  if (precision == 0) return enqueue_sweep<double>(c, c.cur64);
+  return enqueue_sweep<float>(c, c.cur32);
+}
+
+int launch_energy(Ctx &, const double *, double, double *) { return 0; }
+
+}  // namespace umt

@@ -1,0 +1,107 @@
+// umt_common.cuh -- device context shared by the translation units of
+// libumt103.so.  One process-wide context (Teton keeps its mesh, quadrature
+// and angular flux in module state the same way, mods/Geometry_mod.F90,
+// mods/QuadratureList_mod.F90).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#define UMT_MAXCF 3
+#define UMT_MAXCORNER 8
+#define UMT_MAXFACES 6
+
+// device status word bits (sticky until umt103_init / read)
+#define UMT_DEV_CYCLE 1u
+#define UMT_DEV_BOUNDS 2u
+#define UMT_DEV_TIMEOUT 4u
+
+namespace umt {
+
+// Schedule of all directions of the angle set: work items (one per
+// direction x zone) ordered by dependency stage; stage h holds every
+// (direction, zone) whose longest upstream chain has h zones.
+struct Schedule {
+  uint32_t *items = nullptr;      // [A*nz] bit31 = lagged (bad) zone, low bits a*nz+z
+  int *stageCount = nullptr;      // [nz+2]
+  int *stageOffset = nullptr;     // [nz+2]
+  int *need = nullptr;            // [A*nz]
+  uint8_t *exitMask = nullptr;    // [A*nz] bit f: zone face f is an exit face
+  uint8_t *bad = nullptr;         // [A*nz] intra-zone corner cycle
+  uint32_t *order = nullptr;      // [A*nz] corner solve order, 8 nibbles
+  int *level = nullptr;           // [A*nz]
+  int *nHyper = nullptr;          // [A]
+  unsigned long long *processed = nullptr;  // items placed
+  int nStages = 0;
+  std::vector<int> hCount, hOffset;         // host copies
+  int maxStageItems = 0;
+};
+
+struct Ctx {
+  bool ready = false;
+  int nz = 0, nc = 0, nb = 0, A = 0, G = 0;
+  int flags = 0;
+  cudaStream_t stream = nullptr;
+  // mesh (device, 0-based)
+  int *numCorner = nullptr, *cOffSet = nullptr, *zoneFaces = nullptr;
+  int *zoneOpp = nullptr, *faceOpp = nullptr;   // [nz*6]
+  int *nCFaces = nullptr, *cFP = nullptr, *cEZ = nullptr, *CToFace = nullptr; // [nc*3]
+  int *bdyToC = nullptr, *cToZone = nullptr;
+  double *px = nullptr, *A_fp = nullptr, *A_ez = nullptr, *Volume = nullptr;
+  double *VolumeZone = nullptr, *A_bdy = nullptr, *Afp_raw = nullptr;
+  double *omega = nullptr, *weight = nullptr;
+  std::vector<double> h_omega, h_weight;
+  // per-direction corner-face projections Omega.A  [A][nc][3]
+  double *afp64 = nullptr, *aez64 = nullptr;
+  float *afp32 = nullptr, *aez32 = nullptr;
+  Schedule sch;
+  // materials and sources
+  double *Sigt = nullptr, *SigS = nullptr;      // [nz][G]
+  float *Sigt32 = nullptr;
+  double tau = 0.0;
+  double *STotal = nullptr;                     // [nc][G]
+  float *STotal32 = nullptr;
+  double *Phi = nullptr;                        // [nc][G]
+  // angular flux, double buffered: psi[cur] = saved Psi, psi[1-cur] = new
+  double *psi64[2] = {nullptr, nullptr};
+  float *psi32[2] = {nullptr, nullptr};
+  int cur64 = 0, cur32 = 0;
+  double *psiB64 = nullptr;                     // [A][nb][G]
+  float *psiB32 = nullptr;
+  unsigned int *status = nullptr;               // device status word
+  double *scratch = nullptr;                    // reductions
+  size_t scratchBytes = 0;
+  // captured sweep graphs per precision
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float lastMs = -1.f;
+  int sweepGT[2] = {0, 0};                      // group tile per precision
+};
+
+extern Ctx g;
+extern std::string g_err;
+
+int set_error(int code, const char *fmt, ...);
+
+#define UMT_CUDA(call)                                                       \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return set_error(-3, "%s:%d %s: %s", __FILE__, __LINE__, #call,         \
+                       cudaGetErrorString(e_));                              \
+  } while (0)
+
+// launchers (geometry / schedule TU, compiled without FMA contraction)
+int launch_geometry(Ctx &c);
+int launch_projections(Ctx &c);
+int build_schedule(Ctx &c);
+// launchers (sweep TU)
+int capture_sweep_graph(Ctx &c, int precision);
+int launch_sweep_once(Ctx &c, int precision, bool tally);
+int launch_tally(Ctx &c, int precision);
+int launch_convert_source(Ctx &c);
+int launch_energy(Ctx &c, const double *siga_dev, double speed_light, double *out5);
+
+}  // namespace umt
