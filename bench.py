@@ -1,0 +1,310 @@
+"""Benchmark: ns per corner*angle*group of one full UCB sweep on GB300.
+
+Workload (one "step" = one sweep of every direction and group, plus the
+psi->phi tally, on inputs already resident in HBM): the multigroup
+scattering problem of 20x20x20 tiles of the 24-zone tile (192,000 zones,
+1,408,000 corners), 4 polar x 4 azimuthal angles per octant (128
+directions), 16 groups, total opacity log-uniform on [1e-2, 1e2], scattering
+ratio uniform on [0, 0.5], isotropic source 1.0, vacuum boundaries, seeded
+(Philox, seed 2).  Synthetic inputs with the stated shapes and distributions
+stand in for the reference's problem; there is no dataset.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--tiles T] [--precision fp32|fp64]
+
+Multi-GPU: the sweep of one problem does not shard here, so N GPUs run N
+independent replicas (one process per GPU, launched by torchrun); value is
+aggregated over all replicas (units of all ranks / max time over ranks).
+
+--impl reference times the reference algorithm on the host cores: the C++
+restatement of SweepUCBxyz/SetSweep (oracle/), FP64, OpenMP over directions
+with every host thread, on a bounded sample of the same workload (a subset
+of directions on the full mesh), and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ns per corner*angle*group sweep"
+MEASURED = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def b_alg(G: int, A: int, s_psi: int, s_g: int, ncf: int = 3) -> float:
+    """Algorithmic bytes per corner*angle*group: read psi_old, write psi_new,
+    per (corner, angle) geometry amortised over G, per (corner, group) source
+    read and phi write amortised over A."""
+    return 2 * s_psi + (s_g * 6 * ncf + 4 * 2 * ncf + s_g) / G + 16.0 / A
+
+
+def peaks():
+    try:
+        d = json.load(open(MEASURED))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            if len(s) > 8:
+                for k, n in enumerate(names):
+                    if s[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_problem(tiles):
+    from umt_gb300.problems import synthetic_problem
+    return synthetic_problem((tiles,) * 3, 4, 4, 16, seed=2, sigt_range=(1e-2, 1e2), c_range=(0.0, 0.5),
+                             q=1.0, time_dependent=True)
+
+
+def source_from_phi(prob, phi):
+    """STotal = (sigma_s * phi + q)/(4 pi) per corner (isotropic scattering source)."""
+    from umt_gb300.quadrature import WTISO_XYZ
+    m = prob.mesh
+    return WTISO_XYZ * (prob.sigs[m.cToZone] * phi + prob.q_ext[m.cToZone])
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the reference algorithm (oracle port) on the host cores."""
+    if rank != 0:
+        return
+    from oracle import pyoracle as po
+    prob = make_problem(args.tiles)
+    m = prob.mesh
+    A, G = len(prob.weight), prob.ngr
+    nth = os.cpu_count() or 1
+    sample_angles = min(A, max(nth, 16))
+    sel = np.linspace(0, A - 1, sample_angles).round().astype(int)
+    om = np.ascontiguousarray(prob.omega[sel]); w = np.ascontiguousarray(prob.weight[sel])
+    geo = po.geometry(m)
+    S = po.schedule(m, geo[0], geo[1], om)
+    Psi = np.ascontiguousarray(prob.psi0[sel])
+    PsiB = np.zeros((sample_angles, m.nbelem, G))
+    STotal = np.ascontiguousarray(source_from_phi(prob, np.zeros((m.ncornr, G))))
+    sigt = np.ascontiguousarray(prob.sigt)
+    units = m.ncornr * sample_angles * G
+    for _ in range(args.warmup):
+        po.set_sweep(m, geo, S, sigt, STotal, prob.tau, om, w, Psi, PsiB, nthreads=nth)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        po.set_sweep(m, geo, S, sigt, STotal, prob.tau, om, w, Psi, PsiB, nthreads=nth)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    v = t * 1e9 / units
+    line = {"metric": METRIC, "value": v, "unit": "ns", "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"multigroup scattering, {args.tiles}^3 tiles, 128 directions, 16 groups",
+                       "tiles": args.tiles, "directions": A, "groups": G, "zones": m.nzones,
+                       "corners": m.ncornr, "sample_directions": int(sample_angles)},
+            "cpu_baseline": {"value": v, "unit": "ns", "cores": nth, "kind": "port",
+                             "sample": f"{sample_angles} of {A} directions on the full mesh, all groups"},
+            "e2e": {"value": v, "unit": "ns", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(prob, budget_s=20.0):
+    """Oracle FP64 sweep over a few directions on the full mesh (bounded)."""
+    from oracle import pyoracle as po
+    m = prob.mesh
+    G = prob.ngr
+    nth = os.cpu_count() or 1
+    n_ang = max(1, min(len(prob.weight), nth))
+    sel = np.linspace(0, len(prob.weight) - 1, n_ang).round().astype(int)
+    om = np.ascontiguousarray(prob.omega[sel]); w = np.ascontiguousarray(prob.weight[sel])
+    geo = po.geometry(m)
+    S = po.schedule(m, geo[0], geo[1], om)
+    Psi = np.ascontiguousarray(prob.psi0[sel]); PsiB = np.zeros((n_ang, m.nbelem, G))
+    STotal = np.ascontiguousarray(source_from_phi(prob, np.zeros((m.ncornr, G))))
+    sigt = np.ascontiguousarray(prob.sigt)
+    t0 = time.perf_counter(); reps = 0
+    while True:
+        po.set_sweep(m, geo, S, sigt, STotal, prob.tau, om, w, Psi, PsiB, nthreads=nth)
+        reps += 1
+        if time.perf_counter() - t0 > budget_s / 2 or reps >= 3:
+            break
+    t = (time.perf_counter() - t0) / reps
+    return {"value": t * 1e9 / (m.ncornr * n_ang * G), "unit": "ns", "cores": nth, "kind": "port",
+            "sample": f"{n_ang} of {len(prob.weight)} directions on the full mesh, all groups, FP64"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--tiles", type=int, default=20)
+    ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from umt_gb300 import build, capi
+    build.build()
+    lib = capi.Library()
+    lib.select_device(local)
+    prec = capi.UMT_FP32 if args.precision == "fp32" else capi.UMT_FP64
+    prob = make_problem(args.tiles)
+    m = prob.mesh
+    A, G = len(prob.weight), prob.ngr
+    lib.init(m, prob.omega, prob.weight, G, flags=2 if prec == capi.UMT_FP32 else 1)
+    lib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    lib.set_psi(prob.psi0, None)
+    STotal = np.ascontiguousarray(source_from_phi(prob, np.zeros((m.ncornr, G))))
+    lib.set_source(STotal)
+    units = prob.units
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    # ---- device-resident timed region ----
+    for _ in range(args.warmup):
+        lib.sweep_resident(False, prec)
+    barrier()
+    kern_ms, tally_ms, step_ms = [], [], []
+    launches_per_step = lib.launches_per_sweep(prec)
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            lib.sweep_resident(False, prec)
+            t = lib.timing()
+            step_ms.append(t[0]); kern_ms.append(t[1]); tally_ms.append(t[2])
+    barrier()
+    t_step = sum(step_ms) / len(step_ms)
+    if dist:
+        tt = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = t_step * 1e6 / (units * world)
+
+    # ---- end to end through the public API with host buffers ----
+    Phi = np.zeros((m.ncornr, G))
+    PsiB = np.zeros((A, m.nbelem, G))
+    for _ in range(2):
+        lib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=prec)
+    barrier()
+    e2e_steps = max(3, min(args.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Phi = lib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=prec)
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+    barrier()
+    if dist:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    h2d = STotal.nbytes + PsiB.nbytes
+    d2h = Phi.nbytes + PsiB.nbytes
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    s = 4 if prec == capi.UMT_FP32 else 8
+    balg = b_alg(G, A, s, s)
+    k_avg = sum(kern_ms) / len(kern_ms)
+    peak, src = peaks()
+    achieved = balg * units / (k_avg * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "ns", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if prec == capi.UMT_FP32 else "f64", "data": "synthetic",
+        "config": {"workload": f"multigroup scattering sweep, {args.tiles}^3 tiles (24-zone tile), "
+                               f"128 directions, 16 groups",
+                   "tiles": args.tiles, "zones": m.nzones, "corners": m.ncornr, "directions": A,
+                   "groups": G, "units_per_step": units, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (angular flux %.1f GB)" % (A * m.ncornr * G * s / 1e9),
+                   "psi": "fp32" if s == 4 else "fp64", "tallies": "fp64"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": src,
+                     "kernel": "k_sweep (all dependency stages of one sweep)",
+                     "bytes_per_unit": balg, "kernel_ms": k_avg, "tally_ms": sum(tally_ms) / len(tally_ms)},
+        "e2e": {"value": t_e2e * 1e9 / (units * world), "unit": "ns", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline_sample(prob)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -156,6 +156,10 @@ typedef struct UmtEnergyTally {
 
 int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *tally);
 
+/* Same, on the angular flux of the given precision (UMT_FP64 / UMT_FP32). */
+int umt103_tally_precision(const double *siga, double speed_light, int precision,
+                           UmtEnergyTally *tally);
+
 /* Schedule statistics for one direction. */
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);
 
@@ -168,6 +172,26 @@ int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume);
 
 /* Device time of the last umt103_sweep* call in milliseconds, or < 0. */
 double umt103_last_sweep_ms(void);
+
+/* Device times (ms) of the last sweep: [0] whole sweep, [1] the dependency-
+ * stage sweep kernels, [2] the psi->phi tally.  No reference counterpart
+ * (the reference accumulates wall time in SweepTimeCycle, rt/ControlSweep.F90). */
+int umt103_last_timing(double *out3);
+
+/* Group tile of the FP32 sweep: lanes_per_zone lanes share one (direction,
+ * zone) pair and each lane carries groups_per_lane consecutive groups
+ * (lanes_per_zone*groups_per_lane must equal the group count; 0,0 restores
+ * the default).  Set by the autotuner (umt_gb300/autotune.py).  No reference
+ * counterpart: the reference kernel fixes 4 groups x 32 zones per block
+ * (gpu/GPU_SweepUCBxyz.cu:30-31). */
+int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane);
+
+/* Number of kernels one sweep of the given precision launches (>= 0). */
+int umt103_launches_per_sweep(int precision);
+
+/* Make `device` current for the calling thread before umt103_init (one
+ * process per GPU; the reference binds ranks to GPUs the same way). */
+int umt103_select_device(int device);
 
 /* Last error text (static storage). */
 const char *umt103_error_string(void);

@@ -56,11 +56,17 @@ def build_inputs(name):
 
 
 def input_digest(prob, STotal, geo, S):
+    """Hash of the integer inputs (connectivity and schedule)."""
     h = hashlib.sha256()
-    for a in (prob.omega, prob.weight, prob.sigt, STotal, prob.psi0, geo[0], geo[1], geo[2],
-              S.nextZ, S.nextC, S.zonesInPlane, prob.mesh.cFP, prob.mesh.cEZ):
+    for a in (S.nextZ, S.nextC, S.zonesInPlane, prob.mesh.cFP, prob.mesh.cEZ):
         h.update(np.ascontiguousarray(a).tobytes())
     return h.hexdigest()
+
+
+def input_sums(prob, STotal, geo):
+    """Sums of the floating-point inputs (checked to a tolerance)."""
+    return np.array([np.abs(x).sum() for x in (prob.omega, prob.weight, prob.sigt, STotal, prob.psi0,
+                                               geo[0], geo[1], geo[2])])
 
 
 def run(name, outdir):
@@ -78,7 +84,8 @@ def run(name, outdir):
         assert S.zonesInPlane[a, :S.nHyperPlanes[a]].sum() == nz
 
     dev = torch.device("cuda:0")
-    torch.cuda.init()
+    torch.zeros(1, device=dev)          # creates the primary context
+    torch.cuda.synchronize()
     cuda = C.CDLL("libcuda.so.1")
     ctx = C.c_void_p()
     assert cuda.cuCtxGetCurrent(C.byref(ctx)) == 0 and ctx.value
@@ -137,7 +144,7 @@ def run(name, outdir):
         d_nextC = T(S.nextC[a] + 1, i32)
         d_zip = T(S.zonesInPlane[a, :nh], i32)
         d_om = T(prob.omega[a], f64)
-        d_psib = T(PsiB[a], f64)
+        d_psib = T(PsiB[a].reshape(-1), f64)
         d_psi1[nc * G:] = d_psib
         d_src = d_ST.clone()
         d_psi = T(Psi[a], f64)
@@ -155,8 +162,10 @@ def run(name, outdir):
         Psi[a] = d_psi1[:nc * G].cpu().numpy().reshape(nc, G)       # savePsi
     Phi = d_phi.cpu().numpy().reshape(nc, G)
     os.makedirs(outdir, exist_ok=True)
-    np.savez_compressed(os.path.join(outdir, f"ref_sweep_{name}.npz"), Phi=Phi, PsiB=PsiB,
-                        Psi=Psi, digest=np.array(input_digest(prob, STotal, geo, S)))
+    keep = np.arange(0, A, max(1, A // 16))          # a subset of directions keeps the file small
+    np.savez_compressed(os.path.join(outdir, f"ref_sweep_{name}.npz"), Phi=Phi, PsiB=PsiB[keep],
+                        Psi=Psi[keep], keep=keep, digest=np.array(input_digest(prob, STotal, geo, S)),
+                        sums=input_sums(prob, STotal, geo))
     print(name, "Phi sum", Phi.sum())
 
 

@@ -1,0 +1,68 @@
+"""GPU: the reference driver's uniform problem, cycle by cycle, against the
+oracle (PhiTotal, radiation energy and the energy balance of every cycle),
+and source iteration with scattering."""
+import numpy as np
+import pytest
+
+from umt_gb300 import capi
+from umt_gb300.problems import uniform_problem, synthetic_problem
+from umt_gb300.teton import Teton
+from tests.helpers import oracle_cycles, oracle_sweep, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_uniform_problem_cycles_fp64(umtlib):
+    prob = uniform_problem((2, 2, 2), 2, 2, 2)
+    ref = oracle_cycles(prob, 3)
+    t = Teton(prob, capi.UMT_FP64, umtlib)
+    for k in range(3):
+        e = t.radtr()
+        assert e["tempIters"] == 2                       # 2 outer iterations + savePsi sweep
+        assert rel_err(t.PhiTotal, ref[k]["PhiTotal"]) < 1e-12
+        assert abs(e["EnergyRadiation"] / ref[k]["EnergyRadiation"] - 1) < 1e-12
+        assert abs(e["PowerEscape"] / ref[k]["PowerEscape"] - 1) < 1e-12
+        assert abs(e["EnergyCheck"] - ref[k]["EnergyCheck"]) < 1e-12 * e["EnergyRadiation"]
+        # closed balance including absorption: exact up to rounding
+        assert abs(e["EnergyCheckClosed"]) < 1e-11 * e["EnergyRadiation"]
+
+
+def test_uniform_problem_cycles_fp32(umtlib):
+    prob = uniform_problem((2, 2, 2), 2, 2, 2)
+    ref = oracle_cycles(prob, 2)
+    t = Teton(prob, capi.UMT_FP32, umtlib)
+    for k in range(2):
+        e = t.radtr()
+        assert rel_err(t.PhiTotal, ref[k]["PhiTotal"]) < 1e-5
+        assert abs(e["EnergyRadiation"] / ref[k]["EnergyRadiation"] - 1) < 1e-5
+        assert abs(e["EnergyCheckClosed"]) < 1e-4 * e["EnergyRadiation"]
+
+
+def _oracle_si(prob, tol, max_iters=200):
+    m = prob.mesh
+    G = prob.ngr
+    phi = np.zeros((m.ncornr, G))
+    for it in range(max_iters):
+        st = (prob.sigs[m.cToZone] * phi + prob.q_ext[m.cToZone]) / (4 * np.pi)
+        r = oracle_sweep(prob, STotal=st, Psi=prob.psi0, savePsi=False)
+        new = r["Phi"]
+        rel = np.linalg.norm(new - phi) / np.linalg.norm(new)
+        phi = new
+        if rel < tol:
+            return phi, it + 1
+    return phi, max_iters
+
+
+@pytest.mark.parametrize("precision,tol", [(capi.UMT_FP64, 1e-11), (capi.UMT_FP32, 2e-5)])
+def test_source_iteration(umtlib, precision, tol):
+    prob = synthetic_problem((2, 2, 1), 2, 2, 4, seed=9, c_range=(0.0, 0.5), time_dependent=True)
+    phi_ref, it_ref = _oracle_si(prob, 1e-10)
+    m = prob.mesh
+    umtlib.init(m, prob.omega, prob.weight, prob.ngr)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    res = umtlib.source_iterate(precision=precision, rel_tol=1e-10 if precision == 0 else 1e-6,
+                                q_ext=prob.q_ext, save_psi=False, max_iters=200)
+    phi = umtlib.get_phi()
+    assert res["converged"]
+    assert rel_err(phi, phi_ref) < tol

@@ -77,3 +77,23 @@ def test_fp32_sweep_tolerance(umtlib):
     # FP32 sweep arithmetic: stated tolerance 1e-5 relative (max-norm) on phi
     assert rel_err(Phi, ref["Phi"]) < 1e-5
     assert rel_err(Psi, ref["Psi"]) < 1e-4
+
+
+@pytest.mark.parametrize("G,tile", [(16, (16, 1)), (16, (8, 2)), (16, (4, 4)), (2, (1, 2)),
+                                    (2, (2, 1)), (8, (2, 4)), (32, (8, 4))])
+def test_fp32_group_tiles(umtlib, G, tile):
+    """Every group tile of the production FP32 kernel agrees with the oracle."""
+    prob = synthetic_problem((2, 2, 1), 2, 2, G, seed=4, time_dependent=True)
+    m = prob.mesh
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    ref = oracle_sweep(prob, STotal=STotal, Psi=prob.psi0)
+    umtlib.init(m, prob.omega, prob.weight, G)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    umtlib.set_group_tile(*tile)
+    PsiB = np.zeros((len(prob.weight), m.nbelem, G))
+    Phi = umtlib.sweep(STotal, savePsi=True, PsiB=PsiB, precision=capi.UMT_FP32)
+    Psi, _ = umtlib.get_psi(capi.UMT_FP32)
+    assert rel_err(Phi, ref["Phi"]) < 1e-5
+    assert rel_err(Psi, ref["Psi"]) < 1e-4
+    assert rel_err(PsiB, ref["PsiB"]) < 1e-4

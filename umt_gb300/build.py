@@ -23,6 +23,8 @@ UNITS = {
     "capi.cu": [],
     "geom_sched.cu": ["-fmad=false"],
     "sweep.cu": [],
+    "sweep32.cu": [],
+    "si.cu": [],
 }
 
 

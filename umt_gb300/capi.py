@@ -75,10 +75,13 @@ def load():
         for n in ("umt103_init", "umt103_set_materials", "umt103_set_psi", "umt103_get_psi",
                   "umt103_sweep", "umt103_set_source", "umt103_sweep_resident",
                   "umt103_get_phi", "umt103_source_iterate", "umt103_tally",
-                  "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry"):
+                  "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry",
+                  "umt103_last_timing", "umt103_launches_per_sweep", "umt103_select_device",
+                  "umt103_set_group_tile", "umt103_tally_precision"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
+        _lib.umt103_tally_precision.argtypes = [_dp, C.c_double, C.c_int, C.POINTER(UmtEnergyTally)]
     return _lib
 
 
@@ -86,7 +89,8 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_get_psi", "umt103_sweep", "umt103_set_source", "umt103_sweep_resident",
             "umt103_get_phi", "umt103_source_iterate", "umt103_tally", "umt103_schedule_info",
             "umt103_get_schedule", "umt103_get_geometry", "umt103_last_sweep_ms",
-            "umt103_error_string"]
+            "umt103_error_string", "umt103_last_timing", "umt103_launches_per_sweep",
+            "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision"]
 
 
 def check(rc):
@@ -182,6 +186,45 @@ class Library:
         Phi = np.zeros((self.nc, self.G))
         check(self.lib.umt103_get_phi(_d(Phi)))
         return Phi
+
+    def timing(self):
+        out = np.zeros(3)
+        check(self.lib.umt103_last_timing(_d(out)))
+        return out
+
+    def launches_per_sweep(self, precision):
+        n = self.lib.umt103_launches_per_sweep(int(precision))
+        if n < 0:
+            check(n)
+        return n
+
+    def source_iterate(self, precision=UMT_FP64, max_iters=50, rel_tol=1e-8, q_ext=None, save_psi=True,
+                       use_gta=False, allow_notconv=False):
+        q = _c(q_ext, np.float64)
+        prm = UmtSIParams(int(precision), int(max_iters), float(rel_tol), int(bool(use_gta)), _d(q),
+                          int(bool(save_psi)))
+        res = UmtSIResult()
+        rc = self.lib.umt103_source_iterate(C.byref(prm), C.byref(res))
+        if rc != 0 and not (allow_notconv and rc == -8):
+            check(rc)
+        return dict(iterations=res.iterations, sweeps=res.sweeps, rel_change=res.rel_change,
+                    seconds=res.seconds, converged=(rc == 0))
+
+    def tally(self, siga=None, speed_light=299.792458, precision=None):
+        siga = _c(siga, np.float64)
+        t = UmtEnergyTally()
+        if precision is None:
+            check(self.lib.umt103_tally(_d(siga), C.c_double(speed_light), C.byref(t)))
+        else:
+            check(self.lib.umt103_tally_precision(_d(siga), C.c_double(speed_light), int(precision), C.byref(t)))
+        return dict(EnergyRadiation=t.EnergyRadiation, PowerEscape=t.PowerEscape,
+                    PowerIncident=t.PowerIncident, PowerAbsorbed=t.PowerAbsorbed)
+
+    def set_group_tile(self, lanes_per_zone, groups_per_lane):
+        check(self.lib.umt103_set_group_tile(int(lanes_per_zone), int(groups_per_lane)))
+
+    def select_device(self, device):
+        check(self.lib.umt103_select_device(int(device)))
 
     def last_ms(self):
         return float(self.lib.umt103_last_sweep_ms())

@@ -48,14 +48,17 @@ static void free_all() {
   dfree(c.px); dfree(c.A_fp); dfree(c.A_ez); dfree(c.Volume); dfree(c.VolumeZone); dfree(c.A_bdy);
   dfree(c.Afp_raw); dfree(c.omega); dfree(c.weight);
   dfree(c.afp64); dfree(c.aez64); dfree(c.afp32); dfree(c.aez32);
+  dfree(c.rec32); dfree(c.conn32); dfree(c.vol32);
   Schedule &s = c.sch;
   dfree(s.items); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
   dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
+  dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch);
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
+  if (c.evMid) cudaEventDestroy(c.evMid);
   if (c.stream) cudaStreamDestroy(c.stream);
   c = Ctx();
 }
@@ -109,6 +112,7 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   UMT_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
   UMT_CUDA(cudaEventCreate(&c.ev0));
   UMT_CUDA(cudaEventCreate(&c.ev1));
+  UMT_CUDA(cudaEventCreate(&c.evMid));
   TRY(dalloc(&c.status, 1));
   UMT_CUDA(cudaMemset(c.status, 0, sizeof(unsigned)));
 
@@ -319,6 +323,11 @@ static int sweep_core(int savePsi, int precision) {
   UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
   UMT_CUDA(cudaStreamSynchronize(c.stream));
   cudaEventElapsedTime(&c.lastMs, c.ev0, c.ev1);
+  // stage kernels only: the FP32 path records evMid twice (after the source
+  // conversion and after the last stage); the second record wins for the
+  // tally split, the first is folded into the step time
+  cudaEventElapsedTime(&c.lastTallyMs, c.evMid, c.ev1);
+  c.lastKernMs = c.lastMs - c.lastTallyMs;
   if (savePsi) {
     if (precision == UMT_FP64) c.cur64 = 1 - c.cur64;
     else c.cur32 = 1 - c.cur32;
@@ -379,6 +388,35 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
 
 double umt103_last_sweep_ms(void) { return g.lastMs; }
 
+int umt103_last_timing(double *out3) {
+  if (!out3) return set_error(UMT_ERR_ARG, "null output");
+  out3[0] = g.lastMs; out3[1] = g.lastKernMs; out3[2] = g.lastTallyMs;
+  return 0;
+}
+
+int umt103_launches_per_sweep(int precision) {
+  if (precision != 0 && precision != 1) return set_error(UMT_ERR_ARG, "precision");
+  return g.launchesPerSweep[precision];
+}
+
+int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (lanes_per_zone == 0 && groups_per_lane == 0) { c.tileGT = 0; c.tileGPL = 0; return 0; }
+  if (!sweep32_supported(c.G, lanes_per_zone, groups_per_lane))
+    return set_error(UMT_ERR_ARG, "group tile %d x %d does not cover G=%d", lanes_per_zone, groups_per_lane, c.G);
+  c.tileGT = lanes_per_zone; c.tileGPL = groups_per_lane;
+  return 0;
+}
+
+int umt103_select_device(int device) {
+  int n = 0;
+  UMT_CUDA(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return set_error(UMT_ERR_ARG, "device %d of %d", device, n);
+  UMT_CUDA(cudaSetDevice(device));
+  return 0;
+}
+
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles) {
   Ctx &c = g;
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
@@ -408,12 +446,89 @@ int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume) {
   return 0;
 }
 
-int umt103_source_iterate(const UmtSIParams *, UmtSIResult *) {
-  return set_error(UMT_ERR_STATE, "source iteration not built yet");
+int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!prm || !res) return set_error(UMT_ERR_ARG, "null params/result");
+  const int prec = prm->precision;
+  if (prec != UMT_FP64 && prec != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
+  if (prm->use_gta) return set_error(UMT_ERR_ARG, "use_gta: call umt103_source_iterate_gta");
+  const size_t ncG = (size_t)c.nc * c.G, nzG = (size_t)c.nz * c.G;
+  if (!c.PhiPrev) TRY(dalloc(&c.PhiPrev, ncG));
+  if (!c.red) TRY(dalloc(&c.red, 8));
+  const double *q = nullptr;
+  if (prm->q_ext) {
+    if (!c.qExt) TRY(dalloc(&c.qExt, nzG));
+    UMT_CUDA(cudaMemcpy(c.qExt, prm->q_ext, nzG * 8, cudaMemcpyHostToDevice));
+    q = c.qExt;
+  }
+  const int maxit = prm->max_iters > 0 ? prm->max_iters : 50;
+  UMT_CUDA(cudaMemcpyAsync(c.PhiPrev, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+  cudaEvent_t t0, t1;
+  UMT_CUDA(cudaEventCreate(&t0)); UMT_CUDA(cudaEventCreate(&t1));
+  UMT_CUDA(cudaEventRecord(t0, c.stream));
+  int it = 0, sweeps = 0;
+  double rel = 1.0;
+  bool conv = false;
+  while (it < maxit) {
+    ++it;
+    TRY(launch_build_source(c, q));
+    TRY(launch_sweep_once(c, prec, true));
+    ++sweeps;
+    TRY(launch_change_norm(c, c.PhiPrev, c.red));
+    double h[2];
+    UMT_CUDA(cudaMemcpyAsync(h, c.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    UMT_CUDA(cudaStreamSynchronize(c.stream));
+    rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    if (rel < prm->rel_tol) { conv = true; break; }
+  }
+  if (prm->save_psi) {
+    TRY(launch_build_source(c, q));
+    TRY(launch_sweep_once(c, prec, true));
+    ++sweeps;
+    if (prec == UMT_FP64) c.cur64 = 1 - c.cur64; else c.cur32 = 1 - c.cur32;
+  }
+  UMT_CUDA(cudaEventRecord(t1, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0); cudaEventDestroy(t1);
+  res->iterations = it; res->sweeps = sweeps; res->rel_change = rel; res->seconds = ms * 1e-3;
+  return conv ? 0 : set_error(UMT_ERR_NOTCONV, "not converged after %d iterations (rel change %.3e)", it, rel);
 }
 
-int umt103_tally(const double *, double, UmtEnergyTally *) {
-  return set_error(UMT_ERR_STATE, "tally not built yet");
+int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *t) {
+  if (!g.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  return umt103_tally_precision(siga, speed_light, g.psi64[0] ? UMT_FP64 : UMT_FP32, t);
+}
+
+int umt103_tally_precision(const double *siga, double speed_light, int precision, UmtEnergyTally *t) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
+  if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
+  if (!t || !(speed_light > 0.0)) return set_error(UMT_ERR_ARG, "bad tally arguments");
+  if (!c.red) TRY(dalloc(&c.red, 8));
+  const size_t nzG = (size_t)c.nz * c.G;
+  double *dsiga = nullptr;
+  if (siga) {
+    TRY(dalloc(&dsiga, nzG));
+    UMT_CUDA(cudaMemcpy(dsiga, siga, nzG * 8, cudaMemcpyHostToDevice));
+  }
+  int rc = launch_energy(c, dsiga, precision, c.red);
+  double h[4] = {0, 0, 0, 0};
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(h, c.red, 4 * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = set_error(UMT_ERR_CUDA, "tally: %s", cudaGetErrorString(e));
+  }
+  if (dsiga) cudaFree(dsiga);
+  if (rc) return rc;
+  t->EnergyRadiation = h[0] / speed_light;
+  t->PowerAbsorbed = h[1];
+  t->PowerEscape = h[2];
+  t->PowerIncident = h[3];
+  t->Balance = 0.0;
+  return 0;
 }
 
 }  // extern "C"

@@ -196,12 +196,43 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
 
 // psi -> phi tally: PhiTotal(g,c) = sum_a w_a psi_a(g,c), accumulated in FP64
 // (control/getPhiTotal_OMPOL.F90:63-131 does the same per direction).
+// Each thread owns 4 consecutive (corner, group) entries and walks the
+// directions with 4 independent partial sums, so many 128-bit loads are in
+// flight per thread (the pass is bound by reading psi once).
 template <typename T>
-__global__ void k_tally(int A, size_t ncG, const double *weight, const T *psi, double *Phi) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncG; e += (size_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
-    for (int a = 0; a < A; ++a) s += weight[a] * (double)psi[(size_t)a * ncG + e];
-    Phi[e] = s;
+__global__ void __launch_bounds__(256) k_tally(int A, size_t ncG, const double *weight, const T *psi, double *Phi) {
+  const size_t n4 = ncG / 4;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n4; q += (size_t)gridDim.x * blockDim.x) {
+    double s[4][4] = {};
+    int a = 0;
+    for (; a + 4 <= A; a += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const double w = weight[a + u];
+        const T *p = psi + (size_t)(a + u) * ncG + 4 * q;
+        if constexpr (sizeof(T) == 4) {
+          const float4 v = *reinterpret_cast<const float4 *>(p);
+          s[u][0] += w * v.x; s[u][1] += w * v.y; s[u][2] += w * v.z; s[u][3] += w * v.w;
+        } else {
+          const double2 v0 = *reinterpret_cast<const double2 *>(p);
+          const double2 v1 = *reinterpret_cast<const double2 *>(p + 2);
+          s[u][0] += w * v0.x; s[u][1] += w * v0.y; s[u][2] += w * v1.x; s[u][3] += w * v1.y;
+        }
+      }
+    }
+    for (; a < A; ++a) {
+      const double w = weight[a];
+      const T *p = psi + (size_t)a * ncG + 4 * q;
+      for (int j = 0; j < 4; ++j) s[0][j] += w * (double)p[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) Phi[4 * q + j] = (s[0][j] + s[1][j]) + (s[2][j] + s[3][j]);
+  }
+  // remainder entries (ncG not a multiple of 4)
+  for (size_t e = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncG; e += (size_t)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int a = 0; a < A; ++a) t += weight[a] * (double)psi[(size_t)a * ncG + e];
+    Phi[e] = t;
   }
 }
 
@@ -229,6 +260,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
     p.psi_old = (const T *)c.psi32[cur]; p.psi_new = (T *)c.psi32[1 - cur]; p.psiB = (T *)c.psiB32;
   }
   const int prec = sizeof(T) == 8 ? 0 : 1;
+  if constexpr (sizeof(T) == 4) UMT_CUDA(cudaEventRecord(c.evMid, c.stream));
   int GT = c.sweepGT[prec];
   if (GT <= 0) {
     GT = 1;
@@ -236,13 +268,26 @@ static int enqueue_sweep(Ctx &c, int cur) {
     c.sweepGT[prec] = GT;
   }
   const int TEAMS = SWEEP_NT / GT;
+  c.launchesPerSweep[prec] = c.sch.nStages + 1 + (sizeof(T) == 4 ? 2 : 0);
+  bool done = false;
   if constexpr (sizeof(T) == 4) {
     const size_t n = (size_t)c.nz * c.G;
     k_to_float<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(n, c.Sigt, c.Sigt32);
     const size_t m = (size_t)c.nc * c.G;
     k_to_float<<<(int)std::min<size_t>((m + 255) / 256, 4096), 256, 0, c.stream>>>(m, c.STotal, c.STotal32);
+    if (c.tileGT == 0) default_tile(c.G, &c.tileGT, &c.tileGPL);
+    if (c.tileGT > 0 && sweep32_supported(c.G, c.tileGT, c.tileGPL)) {
+      if (!c.rec32Ready) {
+        int rc = prepare_sweep32(c);
+        if (rc) return rc;
+        c.rec32Ready = true;
+      }
+      int rc = enqueue_sweep32(c, cur, c.tileGT, c.tileGPL);
+      if (rc) return rc;
+      done = true;
+    }
   }
-  for (int s = 0; s < c.sch.nStages; ++s) {
+  for (int s = 0; s < c.sch.nStages && !done; ++s) {
     const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;
     switch (GT) {
       case 1: k_sweep<T, 1><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
@@ -253,6 +298,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
       default: k_sweep<T, 32><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
     }
   }
+  UMT_CUDA(cudaEventRecord(c.evMid, c.stream));
   const size_t ncG = (size_t)c.nc * c.G;
   k_tally<T><<<(int)std::min<size_t>((ncG + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
       c.A, ncG, c.weight, (const T *)(sizeof(T) == 8 ? (const void *)c.psi64[1 - cur] : (const void *)c.psi32[1 - cur]), c.Phi);
@@ -265,6 +311,5 @@ int launch_sweep_once(Ctx &c, int precision, bool /*tally*/) {
   return enqueue_sweep<float>(c, c.cur32);
 }
 
-int launch_energy(Ctx &, const double *, double, double *) { return 0; }
 
 }  // namespace umt

@@ -1,0 +1,339 @@
+// sweep32.cu -- production FP32 UCB sweep kernel.
+//
+// Same arithmetic as snac/SweepUCBxyz.F90:103-312, reorganised for SIMT
+// throughput:
+//   * a team of GT lanes owns one (direction, zone) pair and each lane owns
+//     GPL consecutive groups, so every global and shared access of a corner is
+//     one GPL-wide vector per lane and the zone's structure is decoded once per
+//     GPL groups;
+//   * per (direction, corner) the FP and EZ projections and the outflow area
+//     sum are prepacked (CornerRec, 32 B, two 128-bit loads); per corner the
+//     connectivity is packed into one int4 (Conn);
+//   * corner-face slots are walked with fixed trip counts (3 FP + 3 EZ) and
+//     predicates, so lanes of different zones in one warp stay converged;
+//   * the EZ coupling uses the reference's gnum/gden closure with fast
+//     reciprocals (FP32 path; the FP64 path in sweep.cu keeps IEEE division).
+// Corner sources and running sums of the team live in shared memory,
+// [team][corner][group], padded so that teams of one warp fall in different
+// banks.  Every lane touches only its own groups, so no lane waits on another.
+#include "umt_common.cuh"
+
+namespace umt {
+
+struct Sweep32P {
+  int nz, nc, nb, A, G, stride;   // stride: floats per team per array
+  const uint32_t *items;
+  const int *stageOffset, *stageCount;
+  const uint32_t *order;
+  const int *numCorner, *cOffSet;
+  const float4 *rec;     // [A][nc][2]
+  const int4 *conn;      // [nc]
+  const float *vol;      // [nc]
+  const float *Sigt;     // [nz][G]
+  const float *STotal;   // [nc][G]
+  float tau;
+  const float *psi_old;
+  float *psi_new, *psiB;
+};
+
+template <int N> struct VecT;
+template <> struct VecT<1> { using T = float; };
+template <> struct VecT<2> { using T = float2; };
+template <> struct VecT<4> { using T = float4; };
+
+template <int N>
+__device__ __forceinline__ void vload(const float *p, float (&v)[N]) {
+  using V = typename VecT<N>::T;
+  V t = *reinterpret_cast<const V *>(p);
+  const float *f = reinterpret_cast<const float *>(&t);
+#pragma unroll
+  for (int j = 0; j < N; ++j) v[j] = f[j];
+}
+template <int N>
+__device__ __forceinline__ void vstore(float *p, const float (&v)[N]) {
+  using V = typename VecT<N>::T;
+  V t;
+  float *f = reinterpret_cast<float *>(&t);
+#pragma unroll
+  for (int j = 0; j < N; ++j) f[j] = v[j];
+  *reinterpret_cast<V *>(p) = t;
+}
+
+template <int GT, int GPL>
+__global__ void __launch_bounds__(128) k_sweep32(Sweep32P p, int stage) {
+  constexpr int NT = 128, TEAMS = NT / GT;
+  extern __shared__ float smem[];
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const int k = blockIdx.x * TEAMS + team;
+  if (k >= p.stageCount[stage]) return;
+  const int G = GT * GPL;
+  float *sQ = smem + (size_t)team * p.stride;          // [8][G]
+  float *sS = sQ + (size_t)TEAMS * p.stride;           // running corner source
+  uint32_t it = p.items[p.stageOffset[stage] + k];
+  const bool bad = (it >> 31) != 0;
+  it &= 0x7fffffffu;
+  const int a = (int)(it / (uint32_t)p.nz);
+  const int z = (int)(it - (uint32_t)a * p.nz);
+  const int nCorner = p.numCorner[z], c0 = p.cOffSet[z];
+  const uint32_t ord = p.order[it];
+  const int g0 = lane * GPL;
+  const size_t abase = (size_t)a * p.nc;
+
+  float sig[GPL], rsig[GPL];
+  vload<GPL>(p.Sigt + (size_t)z * G + g0, sig);
+#pragma unroll
+  for (int j = 0; j < GPL; ++j) rsig[j] = __frcp_rn(sig[j]);
+
+  // volume sources
+  for (int c = 0; c < nCorner; ++c) {
+    const size_t e = (size_t)(c0 + c) * G + g0;
+    float po[GPL], st[GPL], q[GPL], s[GPL];
+    vload<GPL>(p.psi_old + abase * G + e, po);
+    vload<GPL>(p.STotal + e, st);
+    const float v = p.vol[c0 + c];
+#pragma unroll
+    for (int j = 0; j < GPL; ++j) { q[j] = fmaf(p.tau, po[j], st[j]); s[j] = v * q[j]; }
+    vstore<GPL>(sQ + c * G + g0, q);
+    vstore<GPL>(sS + c * G + g0, s);
+  }
+
+  // incoming FP faces and EZ couplings, corner by corner
+  for (int c = 0; c < nCorner; ++c) {
+    const float4 r0 = p.rec[(abase + c0 + c) * 2 + 0];
+    const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
+    const int4 cn = p.conn[c0 + c];
+    const float afp[3] = {r0.x, r0.y, r0.z};
+    const float aez[3] = {r1.x, r1.y, r1.z};
+    const int cfp[3] = {cn.x, cn.y, cn.z};
+    const int meta = cn.w;
+    const int ncf = meta >> 9;
+    const float vol = r1.w;
+    float src[GPL], Qc[GPL];
+    vload<GPL>(sS + c * G + g0, src);
+    vload<GPL>(sQ + c * G + g0, Qc);
+    float pf[3][GPL];
+#pragma unroll
+    for (int cf = 0; cf < 3; ++cf) {
+#pragma unroll
+      for (int j = 0; j < GPL; ++j) pf[cf][j] = 0.f;
+      if (cf < ncf && afp[cf] < 0.f) {
+        const int up = cfp[cf];
+        const float *src_p = up >= 0 ? p.psi_new + (abase + up) * G + g0
+                                     : p.psiB + ((size_t)a * p.nb + (size_t)(-up - 1)) * G + g0;
+        vload<GPL>(src_p, pf[cf]);
+#pragma unroll
+        for (int j = 0; j < GPL; ++j) src[j] = fmaf(-afp[cf], pf[cf][j], src[j]);
+      }
+    }
+#pragma unroll
+    for (int cf = 0; cf < 3; ++cf) {
+      const float ae = aez[cf];
+      if (cf < ncf && ae > 0.f) {
+        const int cez = (meta >> (3 * cf)) & 7;
+        float Qz[GPL], sz[GPL], sez[GPL];
+        vload<GPL>(sQ + cez * G + g0, Qz);
+        vload<GPL>(sS + cez * G + g0, sz);
+        const int ifp = (cf + 1) % 3;
+        const bool opp = (ncf == 3) && (afp[ifp] < 0.f);
+        if (opp) {
+          const float a2 = ae * ae;
+#pragma unroll
+          for (int j = 0; j < GPL; ++j) {
+            const float sigv = sig[j] * vol;
+            const float sigv2 = sigv * sigv;
+            const float gnum = a2 * (1.82f * sigv2 + ae * (4.f * sigv + 3.f * ae));
+            const float gden = vol * (4.f * sigv * sigv2 + ae * (6.f * sigv2 + 2.f * ae * (2.f * sigv + ae)));
+            const float num = vol * gnum * (sig[j] * pf[ifp][j] - Qc[j]) + 0.5f * ae * gden * (Qc[j] - Qz[j]);
+            sez[j] = __fdividef(num, gnum + gden * sig[j]);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < GPL; ++j) sez[j] = 0.5f * ae * rsig[j] * (Qc[j] - Qz[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < GPL; ++j) { src[j] += sez[j]; sz[j] -= sez[j]; }
+        vstore<GPL>(sS + cez * G + g0, sz);
+      }
+    }
+    vstore<GPL>(sS + c * G + g0, src);
+  }
+
+  float *out = p.psi_new + abase * G + g0;
+  if (!bad) {
+    for (int i = 0; i < nCorner; ++i) {
+      const int c = (int)((ord >> (4 * i)) & 15u);
+      const float4 r0 = p.rec[(abase + c0 + c) * 2 + 0];
+      const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
+      const int4 cn = p.conn[c0 + c];
+      const int ncf = cn.w >> 9;
+      float s[GPL], v[GPL];
+      vload<GPL>(sS + c * G + g0, s);
+#pragma unroll
+      for (int j = 0; j < GPL; ++j) v[j] = __fdividef(s[j], fmaf(sig[j], r1.w, r0.w));
+      vstore<GPL>(out + (size_t)(c0 + c) * G, v);
+      const float aez[3] = {r1.x, r1.y, r1.z};
+      const float afp[3] = {r0.x, r0.y, r0.z};
+      const int cfp[3] = {cn.x, cn.y, cn.z};
+#pragma unroll
+      for (int cf = 0; cf < 3; ++cf) {
+        if (cf < ncf && aez[cf] > 0.f) {
+          const int cez = (cn.w >> (3 * cf)) & 7;
+          float t[GPL];
+          vload<GPL>(sS + cez * G + g0, t);
+#pragma unroll
+          for (int j = 0; j < GPL; ++j) t[j] = fmaf(aez[cf], v[j], t[j]);
+          vstore<GPL>(sS + cez * G + g0, t);
+        }
+        if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f)
+          vstore<GPL>(p.psiB + ((size_t)a * p.nb + (size_t)(-cfp[cf] - 1)) * G + g0, v);
+      }
+    }
+  } else {
+    // direct solve with the previous iterate of the zone's corners
+    for (int c = 0; c < nCorner; ++c) {
+      const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
+      const int4 cn = p.conn[c0 + c];
+      const int ncf = cn.w >> 9;
+      float old[GPL];
+      vload<GPL>(out + (size_t)(c0 + c) * G, old);
+      const float aez[3] = {r1.x, r1.y, r1.z};
+#pragma unroll
+      for (int cf = 0; cf < 3; ++cf)
+        if (cf < ncf && aez[cf] > 0.f) {
+          const int cez = (cn.w >> (3 * cf)) & 7;
+          float t[GPL];
+          vload<GPL>(sS + cez * G + g0, t);
+#pragma unroll
+          for (int j = 0; j < GPL; ++j) t[j] = fmaf(aez[cf], old[j], t[j]);
+          vstore<GPL>(sS + cez * G + g0, t);
+        }
+    }
+    for (int c = 0; c < nCorner; ++c) {
+      const float4 r0 = p.rec[(abase + c0 + c) * 2 + 0];
+      const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
+      const int4 cn = p.conn[c0 + c];
+      const int ncf = cn.w >> 9;
+      float s[GPL], v[GPL];
+      vload<GPL>(sS + c * G + g0, s);
+#pragma unroll
+      for (int j = 0; j < GPL; ++j) v[j] = __fdividef(s[j], fmaf(sig[j], r1.w, r0.w));
+      vstore<GPL>(out + (size_t)(c0 + c) * G, v);
+      const float afp[3] = {r0.x, r0.y, r0.z};
+      const int cfp[3] = {cn.x, cn.y, cn.z};
+#pragma unroll
+      for (int cf = 0; cf < 3; ++cf)
+        if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f)
+          vstore<GPL>(p.psiB + ((size_t)a * p.nb + (size_t)(-cfp[cf] - 1)) * G + g0, v);
+    }
+  }
+}
+
+// Per (direction, corner) record: FP projections, outflow area sum
+// (sumArea of SweepUCBxyz.F90:135-176, summed FP then EZ in face order),
+// EZ projections and the corner volume.
+__global__ void k_corner_rec(int A, int nc, const int *nCFaces, const double *afp64,
+                             const double *aez64, const double *Volume, float4 *rec) {
+  const size_t n = (size_t)A * nc;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % nc);
+    const int ncf = nCFaces[c];
+    float f[3], e[3];
+    float sum = 0.f;
+    for (int cf = 0; cf < 3; ++cf) {
+      f[cf] = cf < ncf ? (float)afp64[i * 3 + cf] : 0.f;
+      if (f[cf] > 0.f) sum += f[cf];
+    }
+    for (int cf = 0; cf < 3; ++cf) {
+      e[cf] = cf < ncf ? (float)aez64[i * 3 + cf] : 0.f;
+      if (e[cf] > 0.f) sum += e[cf];
+    }
+    rec[2 * i] = make_float4(f[0], f[1], f[2], sum);
+    rec[2 * i + 1] = make_float4(e[0], e[1], e[2], (float)Volume[c]);
+  }
+}
+
+__global__ void k_conn(int nc, const int *nCFaces, const int *cFP, const int *cEZ, int4 *conn, float *vol32,
+                       const double *Volume) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int ncf = nCFaces[c];
+    int v[3];
+    int meta = ncf << 9;
+    for (int cf = 0; cf < 3; ++cf) {
+      const int x = cf < ncf ? cFP[c * 3 + cf] : 0;
+      v[cf] = x >= nc ? -(x - nc) - 1 : x;
+      if (cf < ncf) meta |= (cEZ[c * 3 + cf] & 7) << (3 * cf);
+    }
+    conn[c] = make_int4(v[0], v[1], v[2], meta);
+    vol32[c] = (float)Volume[c];
+  }
+}
+
+int prepare_sweep32(Ctx &c) {
+  if (!c.rec32) {
+    cudaError_t e1 = cudaMalloc((void **)&c.rec32, (size_t)c.A * c.nc * 2 * sizeof(float4));
+    cudaError_t e2 = cudaMalloc((void **)&c.conn32, (size_t)c.nc * sizeof(int4));
+    cudaError_t e3 = cudaMalloc((void **)&c.vol32, (size_t)c.nc * sizeof(float));
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+      return set_error(-7, "allocation of the FP32 corner records failed");
+  }
+  const size_t n = (size_t)c.A * c.nc;
+  k_corner_rec<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
+      c.A, c.nc, c.nCFaces, c.afp64, c.aez64, c.Volume, (float4 *)c.rec32);
+  k_conn<<<(c.nc + 255) / 256, 256, 0, c.stream>>>(c.nc, c.nCFaces, c.cFP, c.cEZ, (int4 *)c.conn32, c.vol32,
+                                                   c.Volume);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// Group tile: GT lanes per (direction, zone), GPL groups per lane, G = GT*GPL.
+bool sweep32_supported(int G, int GT, int GPL) {
+  return GT * GPL == G && (GT == 1 || GT == 2 || GT == 4 || GT == 8 || GT == 16 || GT == 32) &&
+         (GPL == 1 || GPL == 2 || GPL == 4);
+}
+
+void default_tile(int G, int *GT, int *GPL) {
+  *GT = 0; *GPL = 0;
+  for (int gpl = 4; gpl >= 1; gpl /= 2)
+    if (G % gpl == 0 && sweep32_supported(G, G / gpl, gpl)) { *GT = G / gpl; *GPL = gpl; return; }
+}
+
+static int team_stride(int G) {
+  const int base = 8 * G;
+  return base + (((G - (base % 32)) % 32) + 32) % 32;
+}
+
+int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
+  Sweep32P p;
+  p.nz = c.nz; p.nc = c.nc; p.nb = c.nb; p.A = c.A; p.G = c.G; p.stride = team_stride(c.G);
+  p.items = c.sch.items; p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
+  p.order = c.sch.order; p.numCorner = c.numCorner; p.cOffSet = c.cOffSet;
+  p.rec = (const float4 *)c.rec32; p.conn = (const int4 *)c.conn32; p.vol = c.vol32;
+  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
+  p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
+  const int TEAMS = 128 / GT;
+  const size_t smem = (size_t)2 * TEAMS * p.stride * sizeof(float);
+#define UMT_LAUNCH32(gt, gpl)                                                                      \
+  if (GT == gt && GPL == gpl) {                                                                    \
+    static bool attr = false;                                                                      \
+    if (!attr) {                                                                                   \
+      cudaFuncSetAttribute(k_sweep32<gt, gpl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); \
+      attr = true;                                                                                 \
+    }                                                                                              \
+    for (int s = 0; s < c.sch.nStages; ++s) {                                                      \
+      const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                    \
+      k_sweep32<gt, gpl><<<blocks, 128, smem, c.stream>>>(p, s);                                   \
+    }                                                                                              \
+    UMT_CUDA(cudaGetLastError());                                                                  \
+    return 0;                                                                                      \
+  }
+  UMT_LAUNCH32(1, 1) UMT_LAUNCH32(1, 2) UMT_LAUNCH32(1, 4)
+  UMT_LAUNCH32(2, 1) UMT_LAUNCH32(2, 2) UMT_LAUNCH32(2, 4)
+  UMT_LAUNCH32(4, 1) UMT_LAUNCH32(4, 2) UMT_LAUNCH32(4, 4)
+  UMT_LAUNCH32(8, 1) UMT_LAUNCH32(8, 2) UMT_LAUNCH32(8, 4)
+  UMT_LAUNCH32(16, 1) UMT_LAUNCH32(16, 2) UMT_LAUNCH32(16, 4)
+  UMT_LAUNCH32(32, 1) UMT_LAUNCH32(32, 2) UMT_LAUNCH32(32, 4)
+#undef UMT_LAUNCH32
+  return set_error(-1, "unsupported group tile GT=%d GPL=%d", GT, GPL);
+}
+
+}  // namespace umt

@@ -56,6 +56,12 @@ struct Ctx {
   // per-direction corner-face projections Omega.A  [A][nc][3]
   double *afp64 = nullptr, *aez64 = nullptr;
   float *afp32 = nullptr, *aez32 = nullptr;
+  // packed records of the production FP32 kernel (sweep32.cu)
+  void *rec32 = nullptr;                        // [A][nc] 2 x float4
+  void *conn32 = nullptr;                       // [nc] int4
+  float *vol32 = nullptr;                       // [nc]
+  bool rec32Ready = false;
+  int tileGT = 0, tileGPL = 0;                  // FP32 group tile (0: choose)
   Schedule sch;
   // materials and sources
   double *Sigt = nullptr, *SigS = nullptr;      // [nz][G]
@@ -64,6 +70,9 @@ struct Ctx {
   double *STotal = nullptr;                     // [nc][G]
   float *STotal32 = nullptr;
   double *Phi = nullptr;                        // [nc][G]
+  double *PhiPrev = nullptr;                    // [nc][G] previous iterate
+  double *qExt = nullptr;                       // [nz][G] isotropic source
+  double *red = nullptr;                        // [8] reduction slots
   // angular flux, double buffered: psi[cur] = saved Psi, psi[1-cur] = new
   double *psi64[2] = {nullptr, nullptr};
   float *psi32[2] = {nullptr, nullptr};
@@ -75,8 +84,9 @@ struct Ctx {
   size_t scratchBytes = 0;
   // captured sweep graphs per precision
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  float lastMs = -1.f;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evMid = nullptr;
+  float lastMs = -1.f, lastKernMs = -1.f, lastTallyMs = -1.f;
+  int launchesPerSweep[2] = {0, 0};
   int sweepGT[2] = {0, 0};                      // group tile per precision
 };
 
@@ -102,6 +112,14 @@ int capture_sweep_graph(Ctx &c, int precision);
 int launch_sweep_once(Ctx &c, int precision, bool tally);
 int launch_tally(Ctx &c, int precision);
 int launch_convert_source(Ctx &c);
-int launch_energy(Ctx &c, const double *siga_dev, double speed_light, double *out5);
+// source iteration and edits (si.cu)
+int launch_build_source(Ctx &c, const double *q);
+int launch_change_norm(Ctx &c, double *prev, double *out2);
+int launch_energy(Ctx &c, const double *siga_dev, int precision, double *out4);
+// production FP32 kernel (sweep32.cu)
+int prepare_sweep32(Ctx &c);
+bool sweep32_supported(int G, int GT, int GPL);
+int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL);
+void default_tile(int G, int *GT, int *GPL);
 
 }  // namespace umt
