@@ -42,7 +42,8 @@ static void dfree(T *&p) {
 static void free_all() {
   Ctx &c = g;
   for (int i = 0; i < 2; ++i)
-    if (c.graph[i]) { cudaGraphExecDestroy(c.graph[i]); c.graph[i] = nullptr; }
+    for (int j = 0; j < 2; ++j)
+      if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
   dfree(c.numCorner); dfree(c.cOffSet); dfree(c.zoneFaces); dfree(c.zoneOpp); dfree(c.faceOpp);
   dfree(c.nCFaces); dfree(c.cFP); dfree(c.cEZ); dfree(c.CToFace); dfree(c.bdyToC); dfree(c.cToZone);
   dfree(c.px); dfree(c.A_fp); dfree(c.A_ez); dfree(c.Volume); dfree(c.VolumeZone); dfree(c.A_bdy);
@@ -50,7 +51,7 @@ static void free_all() {
   dfree(c.afp64); dfree(c.aez64); dfree(c.afp32); dfree(c.aez32);
   dfree(c.rec32); dfree(c.conn32); dfree(c.vol32);
   Schedule &s = c.sch;
-  dfree(s.items); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
+  dfree(s.items); dfree(s.items2); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
   dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red);
@@ -95,6 +96,7 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   const int nz = m->nzones, nc = m->ncornr, nb = m->nbelem, A = q->nangles, G = ngr;
   if (nz <= 0 || nc <= 0 || nb < 0) return set_error(UMT_ERR_ARG, "bad mesh sizes");
   if ((size_t)A * nz >= (1ull << 31)) return set_error(UMT_ERR_ARG, "nangles*nzones must be < 2^31");
+  if (nc >= (1 << 28)) return set_error(UMT_ERR_ARG, "ncornr must be < 2^28");
   if (!m->px && !(m->A_fp && m->A_ez && m->Volume))
     return set_error(UMT_ERR_ARG, "either px or A_fp/A_ez/Volume must be given");
   const int base = m->index_base;
@@ -213,7 +215,7 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   // ---- schedule ----
   Schedule &s = c.sch;
   const size_t nAZ = (size_t)A * nz;
-  TRY(dalloc(&s.items, nAZ)); TRY(dalloc(&s.stageCount, nz + 2)); TRY(dalloc(&s.stageOffset, nz + 2));
+  TRY(dalloc(&s.items, nAZ)); TRY(dalloc(&s.items2, nAZ)); TRY(dalloc(&s.stageCount, nz + 2)); TRY(dalloc(&s.stageOffset, nz + 2));
   TRY(dalloc(&s.need, nAZ)); TRY(dalloc(&s.exitMask, (nAZ + 3) & ~(size_t)3)); TRY(dalloc(&s.bad, nAZ));
   TRY(dalloc(&s.order, nAZ)); TRY(dalloc(&s.level, nAZ)); TRY(dalloc(&s.nHyper, A));
   TRY(dalloc(&s.processed, 1));
@@ -251,6 +253,7 @@ int umt103_set_materials(const double *sigt, const double *sigs, double tau) {
   UMT_CUDA(cudaMemcpy(c.Sigt, sigt, nzG * 8, cudaMemcpyHostToDevice));
   if (sigs) UMT_CUDA(cudaMemcpy(c.SigS, sigs, nzG * 8, cudaMemcpyHostToDevice));
   else UMT_CUDA(cudaMemset(c.SigS, 0, nzG * 8));
+  if (c.tau != tau) invalidate_graphs(c);   // tau is a captured kernel argument
   c.tau = tau;
   return 0;
 }
@@ -402,6 +405,7 @@ int umt103_launches_per_sweep(int precision) {
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane) {
   Ctx &c = g;
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  invalidate_graphs(c);
   if (lanes_per_zone == 0 && groups_per_lane == 0) { c.tileGT = 0; c.tileGPL = 0; return 0; }
   if (!sweep32_supported(c.G, lanes_per_zone, groups_per_lane))
     return set_error(UMT_ERR_ARG, "group tile %d x %d does not cover G=%d", lanes_per_zone, groups_per_lane, c.G);
@@ -518,7 +522,8 @@ int umt103_tally_precision(const double *siga, double speed_light, int precision
   int rc = launch_energy(c, dsiga, precision, c.red);
   double h[4] = {0, 0, 0, 0};
   if (!rc) {
-    cudaError_t e = cudaMemcpy(h, c.red, 4 * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpyAsync(h, c.red, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
     if (e != cudaSuccess) rc = set_error(UMT_ERR_CUDA, "tally: %s", cudaGetErrorString(e));
   }
   if (dsiga) cudaFree(dsiga);

@@ -333,6 +333,17 @@ __global__ void k_stage(int h, int nz, int A, const int *zoneFaces, const int *z
   }
 }
 
+// Items with the zone's corner offset and count packed alongside, so a sweep
+// team learns everything it needs to address its zone from one 64-bit load.
+__global__ void k_items2(size_t n, int nz, const uint32_t *items, const int *cOffSet, const int *numCorner,
+                         uint2 *items2) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t it = items[i];
+    const int z = (int)((it & 0x7fffffffu) % (uint32_t)nz);
+    items2[i] = make_uint2(it, (uint32_t)cOffSet[z] | ((uint32_t)numCorner[z] << 28));
+  }
+}
+
 int build_schedule(Ctx &c) {
   Schedule &s = c.sch;
   const size_t n = (size_t)c.A * c.nz;
@@ -372,6 +383,11 @@ int build_schedule(Ctx &c) {
     if (placed == n) break;
     if (lastCount == 0 || h >= c.nz)
       return set_error(-4, "schedule stalled after %d stages (%llu of %zu items): mesh cycle", h, placed, n);
+  }
+  {
+    const int B2 = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+    k_items2<<<B2, 256, 0, c.stream>>>(n, c.nz, s.items, c.cOffSet, c.numCorner, s.items2);
+    UMT_CUDA(cudaGetLastError());
   }
   s.hCount.assign(c.nz + 2, 0);
   s.hOffset.assign(c.nz + 2, 0);

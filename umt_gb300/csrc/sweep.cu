@@ -18,6 +18,8 @@
 
 namespace umt {
 
+#define TRY_RC(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
+
 template <typename T>
 struct SweepP {
   int nz, nc, nb, A, G;
@@ -260,7 +262,6 @@ static int enqueue_sweep(Ctx &c, int cur) {
     p.psi_old = (const T *)c.psi32[cur]; p.psi_new = (T *)c.psi32[1 - cur]; p.psiB = (T *)c.psiB32;
   }
   const int prec = sizeof(T) == 8 ? 0 : 1;
-  if constexpr (sizeof(T) == 4) UMT_CUDA(cudaEventRecord(c.evMid, c.stream));
   int GT = c.sweepGT[prec];
   if (GT <= 0) {
     GT = 1;
@@ -298,7 +299,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
       default: k_sweep<T, 32><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
     }
   }
-  UMT_CUDA(cudaEventRecord(c.evMid, c.stream));
+  TRY_RC(record_mid(c));
   const size_t ncG = (size_t)c.nc * c.G;
   k_tally<T><<<(int)std::min<size_t>((ncG + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
       c.A, ncG, c.weight, (const T *)(sizeof(T) == 8 ? (const void *)c.psi64[1 - cur] : (const void *)c.psi32[1 - cur]), c.Phi);
@@ -306,7 +307,56 @@ static int enqueue_sweep(Ctx &c, int cur) {
   return 0;
 }
 
+int record_mid(Ctx &c) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  UMT_CUDA(cudaStreamIsCapturing(c.stream, &st));
+  if (st == cudaStreamCaptureStatusActive)
+    UMT_CUDA(cudaEventRecordWithFlags(c.evMid, c.stream, cudaEventRecordExternal));
+  else
+    UMT_CUDA(cudaEventRecord(c.evMid, c.stream));
+  return 0;
+}
+
+void invalidate_graphs(Ctx &c) {
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j)
+      if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
+}
+
+// Capture one sweep (source conversion, every dependency stage, tally) for
+// the current precision and buffer parity into a CUDA graph, once; later
+// sweeps replay it with a single launch.
+static int sweep_via_graph(Ctx &c, int precision) {
+  const int cur = precision == 0 ? c.cur64 : c.cur32;
+  cudaGraphExec_t &ex = c.graphs[precision][cur];
+  if (!ex) {
+    cudaGraph_t gr = nullptr;
+    UMT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    int rc = precision == 0 ? enqueue_sweep<double>(c, cur) : enqueue_sweep<float>(c, cur);
+    cudaError_t e = cudaStreamEndCapture(c.stream, &gr);
+    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+    if (e != cudaSuccess) return set_error(-3, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&ex, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) { ex = nullptr; return set_error(-3, "graph instantiate: %s", cudaGetErrorString(e)); }
+  }
+  UMT_CUDA(cudaGraphLaunch(ex, c.stream));
+  return 0;
+}
+
 int launch_sweep_once(Ctx &c, int precision, bool /*tally*/) {
+  if (c.useGraphs) {
+    // one-time preparation must not be captured
+    if (precision == 1) {
+      if (c.tileGT == 0) default_tile(c.G, &c.tileGT, &c.tileGPL);
+      if (!c.rec32Ready && c.tileGT > 0) {
+        int rc = prepare_sweep32(c);
+        if (rc) return rc;
+        c.rec32Ready = true;
+      }
+    }
+    return sweep_via_graph(c, precision);
+  }
   if (precision == 0) return enqueue_sweep<double>(c, c.cur64);
   return enqueue_sweep<float>(c, c.cur32);
 }

@@ -1,34 +1,37 @@
 // sweep32.cu -- production FP32 UCB sweep kernel.
 //
-// Same arithmetic as snac/SweepUCBxyz.F90:103-312, reorganised for SIMT
-// throughput:
+// Same arithmetic as snac/SweepUCBxyz.F90:103-312, reorganised for latency and
+// SIMT throughput:
 //   * a team of GT lanes owns one (direction, zone) pair and each lane owns
 //     GPL consecutive groups, so every global and shared access of a corner is
-//     one GPL-wide vector per lane and the zone's structure is decoded once per
-//     GPL groups;
-//   * per (direction, corner) the FP and EZ projections and the outflow area
-//     sum are prepacked (CornerRec, 32 B, two 128-bit loads); per corner the
-//     connectivity is packed into one int4 (Conn);
+//     one GPL-wide vector per lane;
+//   * a zone costs three dependent memory round trips: (1) the packed work
+//     item {direction, zone, corner offset, corner count}; (2) at once, the
+//     zone's corner records staged cooperatively into shared memory, and every
+//     corner's previous-cycle flux and source (loops over the 8 corner slots
+//     are unrolled and predicated); (3) at once, every upwind flux of the zone;
+//   * per (direction, corner) the FP and EZ projections, the outflow area sum
+//     and the corner volume are prepacked (two float4), per corner the
+//     connectivity is one int4;
 //   * corner-face slots are walked with fixed trip counts (3 FP + 3 EZ) and
 //     predicates, so lanes of different zones in one warp stay converged;
 //   * the EZ coupling uses the reference's gnum/gden closure with fast
-//     reciprocals (FP32 path; the FP64 path in sweep.cu keeps IEEE division).
-// Corner sources and running sums of the team live in shared memory,
-// [team][corner][group], padded so that teams of one warp fall in different
-// banks.  Every lane touches only its own groups, so no lane waits on another.
+//     reciprocals (the FP64 parity path in sweep.cu keeps IEEE division).
+// Corner sources and running sums live in shared memory, [team][corner][group],
+// padded so that the teams of one warp fall in different banks.  Each lane
+// touches only its own groups there; the staged corner records are shared by
+// the team and published with one __syncwarp over the team's lanes.
 #include "umt_common.cuh"
 
 namespace umt {
 
 struct Sweep32P {
   int nz, nc, nb, A, G, stride;   // stride: floats per team per array
-  const uint32_t *items;
+  const uint2 *items2;
   const int *stageOffset, *stageCount;
   const uint32_t *order;
-  const int *numCorner, *cOffSet;
   const float4 *rec;     // [A][nc][2]
   const int4 *conn;      // [nc]
-  const float *vol;      // [nc]
   const float *Sigt;     // [nz][G]
   const float *STotal;   // [nc][G]
   float tau;
@@ -59,112 +62,143 @@ __device__ __forceinline__ void vstore(float *p, const float (&v)[N]) {
   *reinterpret_cast<V *>(p) = t;
 }
 
+constexpr int SW32_NT = 128;
+
 template <int GT, int GPL>
-__global__ void __launch_bounds__(128) k_sweep32(Sweep32P p, int stage) {
-  constexpr int NT = 128, TEAMS = NT / GT;
-  extern __shared__ float smem[];
+__global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
+  constexpr int TEAMS = SW32_NT / GT;
+  extern __shared__ float4 smem4[];
+  __shared__ float4 sRec[TEAMS][UMT_MAXCORNER][2];
+  __shared__ int4 sConn[TEAMS][UMT_MAXCORNER];
   const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
   const int k = blockIdx.x * TEAMS + team;
-  if (k >= p.stageCount[stage]) return;
+  if (k >= p.stageCount[stage]) return;            // whole teams leave together
+  const unsigned teammask = (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
   const int G = GT * GPL;
-  float *sQ = smem + (size_t)team * p.stride;          // [8][G]
-  float *sS = sQ + (size_t)TEAMS * p.stride;           // running corner source
-  uint32_t it = p.items[p.stageOffset[stage] + k];
-  const bool bad = (it >> 31) != 0;
-  it &= 0x7fffffffu;
+  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.stride;   // [8][G]
+  float *sS = sQ + (size_t)TEAMS * p.stride;                                 // running source
+  // ---- round trip 1: the work item ----
+  const uint2 w = p.items2[p.stageOffset[stage] + k];
+  const bool bad = (w.x >> 31) != 0;
+  const uint32_t it = w.x & 0x7fffffffu;
   const int a = (int)(it / (uint32_t)p.nz);
   const int z = (int)(it - (uint32_t)a * p.nz);
-  const int nCorner = p.numCorner[z], c0 = p.cOffSet[z];
-  const uint32_t ord = p.order[it];
+  const int c0 = (int)(w.y & 0x0fffffffu), nC = (int)(w.y >> 28);
   const int g0 = lane * GPL;
   const size_t abase = (size_t)a * p.nc;
-
+  // ---- round trip 2: structure (cooperative), sources, cross sections ----
+  for (int e = lane; e < 3 * nC; e += GT) {
+    if (e < 2 * nC) sRec[team][e >> 1][e & 1] = p.rec[(abase + c0) * 2 + e];
+    else sConn[team][e - 2 * nC] = p.conn[c0 + e - 2 * nC];
+  }
+  float po[UMT_MAXCORNER][GPL], st[UMT_MAXCORNER][GPL];
+#pragma unroll
+  for (int c = 0; c < UMT_MAXCORNER; ++c) {
+    if (c < nC) {
+      const size_t e = (size_t)(c0 + c) * G + g0;
+      vload<GPL>(p.psi_old + abase * G + e, po[c]);
+      vload<GPL>(p.STotal + e, st[c]);
+    }
+  }
   float sig[GPL], rsig[GPL];
   vload<GPL>(p.Sigt + (size_t)z * G + g0, sig);
+  const uint32_t ord = p.order[it];
+  __syncwarp(teammask);
 #pragma unroll
   for (int j = 0; j < GPL; ++j) rsig[j] = __frcp_rn(sig[j]);
-
-  // volume sources
-  for (int c = 0; c < nCorner; ++c) {
-    const size_t e = (size_t)(c0 + c) * G + g0;
-    float po[GPL], st[GPL], q[GPL], s[GPL];
-    vload<GPL>(p.psi_old + abase * G + e, po);
-    vload<GPL>(p.STotal + e, st);
-    const float v = p.vol[c0 + c];
 #pragma unroll
-    for (int j = 0; j < GPL; ++j) { q[j] = fmaf(p.tau, po[j], st[j]); s[j] = v * q[j]; }
-    vstore<GPL>(sQ + c * G + g0, q);
-    vstore<GPL>(sS + c * G + g0, s);
+  for (int c = 0; c < UMT_MAXCORNER; ++c) {
+    if (c < nC) {
+      const float v = sRec[team][c][1].w;
+      float q[GPL], s[GPL];
+#pragma unroll
+      for (int j = 0; j < GPL; ++j) { q[j] = fmaf(p.tau, po[c][j], st[c][j]); s[j] = v * q[j]; }
+      vstore<GPL>(sQ + c * G + g0, q);
+      vstore<GPL>(sS + c * G + g0, s);
+    }
   }
-
-  // incoming FP faces and EZ couplings, corner by corner
-  for (int c = 0; c < nCorner; ++c) {
-    const float4 r0 = p.rec[(abase + c0 + c) * 2 + 0];
-    const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
-    const int4 cn = p.conn[c0 + c];
+  // ---- round trip 3: every upwind flux of the zone ----
+  float pf[UMT_MAXCORNER][3][GPL];
+#pragma unroll
+  for (int c = 0; c < UMT_MAXCORNER; ++c) {
+    const float4 r0 = sRec[team][c][0];
+    const int4 cn = sConn[team][c];
     const float afp[3] = {r0.x, r0.y, r0.z};
-    const float aez[3] = {r1.x, r1.y, r1.z};
     const int cfp[3] = {cn.x, cn.y, cn.z};
-    const int meta = cn.w;
-    const int ncf = meta >> 9;
-    const float vol = r1.w;
-    float src[GPL], Qc[GPL];
-    vload<GPL>(sS + c * G + g0, src);
-    vload<GPL>(sQ + c * G + g0, Qc);
-    float pf[3][GPL];
+    const int ncf = cn.w >> 9;
 #pragma unroll
     for (int cf = 0; cf < 3; ++cf) {
 #pragma unroll
-      for (int j = 0; j < GPL; ++j) pf[cf][j] = 0.f;
-      if (cf < ncf && afp[cf] < 0.f) {
+      for (int j = 0; j < GPL; ++j) pf[c][cf][j] = 0.f;
+      if (c < nC && cf < ncf && afp[cf] < 0.f) {
         const int up = cfp[cf];
         const float *src_p = up >= 0 ? p.psi_new + (abase + up) * G + g0
                                      : p.psiB + ((size_t)a * p.nb + (size_t)(-up - 1)) * G + g0;
-        vload<GPL>(src_p, pf[cf]);
-#pragma unroll
-        for (int j = 0; j < GPL; ++j) src[j] = fmaf(-afp[cf], pf[cf][j], src[j]);
+        vload<GPL>(src_p, pf[c][cf]);
       }
     }
-#pragma unroll
-    for (int cf = 0; cf < 3; ++cf) {
-      const float ae = aez[cf];
-      if (cf < ncf && ae > 0.f) {
-        const int cez = (meta >> (3 * cf)) & 7;
-        float Qz[GPL], sz[GPL], sez[GPL];
-        vload<GPL>(sQ + cez * G + g0, Qz);
-        vload<GPL>(sS + cez * G + g0, sz);
-        const int ifp = (cf + 1) % 3;
-        const bool opp = (ncf == 3) && (afp[ifp] < 0.f);
-        if (opp) {
-          const float a2 = ae * ae;
-#pragma unroll
-          for (int j = 0; j < GPL; ++j) {
-            const float sigv = sig[j] * vol;
-            const float sigv2 = sigv * sigv;
-            const float gnum = a2 * (1.82f * sigv2 + ae * (4.f * sigv + 3.f * ae));
-            const float gden = vol * (4.f * sigv * sigv2 + ae * (6.f * sigv2 + 2.f * ae * (2.f * sigv + ae)));
-            const float num = vol * gnum * (sig[j] * pf[ifp][j] - Qc[j]) + 0.5f * ae * gden * (Qc[j] - Qz[j]);
-            sez[j] = __fdividef(num, gnum + gden * sig[j]);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < GPL; ++j) sez[j] = 0.5f * ae * rsig[j] * (Qc[j] - Qz[j]);
-        }
-#pragma unroll
-        for (int j = 0; j < GPL; ++j) { src[j] += sez[j]; sz[j] -= sez[j]; }
-        vstore<GPL>(sS + cez * G + g0, sz);
-      }
-    }
-    vstore<GPL>(sS + c * G + g0, src);
   }
-
+  // ---- incoming FP faces and EZ couplings, corner by corner ----
+#pragma unroll
+  for (int c = 0; c < UMT_MAXCORNER; ++c) {
+    if (c < nC) {
+      const float4 r0 = sRec[team][c][0];
+      const float4 r1 = sRec[team][c][1];
+      const int4 cn = sConn[team][c];
+      const float afp[3] = {r0.x, r0.y, r0.z};
+      const float aez[3] = {r1.x, r1.y, r1.z};
+      const int meta = cn.w;
+      const int ncf = meta >> 9;
+      const float vol = r1.w;
+      float src[GPL], Qc[GPL];
+      vload<GPL>(sS + c * G + g0, src);
+      vload<GPL>(sQ + c * G + g0, Qc);
+#pragma unroll
+      for (int cf = 0; cf < 3; ++cf)
+        if (cf < ncf && afp[cf] < 0.f)
+#pragma unroll
+          for (int j = 0; j < GPL; ++j) src[j] = fmaf(-afp[cf], pf[c][cf][j], src[j]);
+#pragma unroll
+      for (int cf = 0; cf < 3; ++cf) {
+        const float ae = aez[cf];
+        if (cf < ncf && ae > 0.f) {
+          const int cez = (meta >> (3 * cf)) & 7;
+          float Qz[GPL], sz[GPL], sez[GPL];
+          vload<GPL>(sQ + cez * G + g0, Qz);
+          vload<GPL>(sS + cez * G + g0, sz);
+          const int ifp = (cf + 1) % 3;
+          if (ncf == 3 && afp[ifp] < 0.f) {
+            const float a2 = ae * ae;
+#pragma unroll
+            for (int j = 0; j < GPL; ++j) {
+              const float sigv = sig[j] * vol;
+              const float sigv2 = sigv * sigv;
+              const float gnum = a2 * (1.82f * sigv2 + ae * (4.f * sigv + 3.f * ae));
+              const float gden = vol * (4.f * sigv * sigv2 + ae * (6.f * sigv2 + 2.f * ae * (2.f * sigv + ae)));
+              const float num = vol * gnum * (sig[j] * pf[c][ifp][j] - Qc[j]) + 0.5f * ae * gden * (Qc[j] - Qz[j]);
+              sez[j] = __fdividef(num, gnum + gden * sig[j]);
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < GPL; ++j) sez[j] = 0.5f * ae * rsig[j] * (Qc[j] - Qz[j]);
+          }
+#pragma unroll
+          for (int j = 0; j < GPL; ++j) { src[j] += sez[j]; sz[j] -= sez[j]; }
+          vstore<GPL>(sS + cez * G + g0, sz);
+        }
+      }
+      vstore<GPL>(sS + c * G + g0, src);
+    }
+  }
+  // ---- corner solve in the schedule's order, exits ----
   float *out = p.psi_new + abase * G + g0;
+  float *outB = p.psiB + (size_t)a * p.nb * G + g0;
   if (!bad) {
-    for (int i = 0; i < nCorner; ++i) {
+    for (int i = 0; i < nC; ++i) {
       const int c = (int)((ord >> (4 * i)) & 15u);
-      const float4 r0 = p.rec[(abase + c0 + c) * 2 + 0];
-      const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
-      const int4 cn = p.conn[c0 + c];
+      const float4 r0 = sRec[team][c][0];
+      const float4 r1 = sRec[team][c][1];
+      const int4 cn = sConn[team][c];
       const int ncf = cn.w >> 9;
       float s[GPL], v[GPL];
       vload<GPL>(sS + c * G + g0, s);
@@ -184,20 +218,18 @@ __global__ void __launch_bounds__(128) k_sweep32(Sweep32P p, int stage) {
           for (int j = 0; j < GPL; ++j) t[j] = fmaf(aez[cf], v[j], t[j]);
           vstore<GPL>(sS + cez * G + g0, t);
         }
-        if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f)
-          vstore<GPL>(p.psiB + ((size_t)a * p.nb + (size_t)(-cfp[cf] - 1)) * G + g0, v);
+        if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f) vstore<GPL>(outB + (size_t)(-cfp[cf] - 1) * G, v);
       }
     }
   } else {
     // direct solve with the previous iterate of the zone's corners
-    for (int c = 0; c < nCorner; ++c) {
-      const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
-      const int4 cn = p.conn[c0 + c];
+    for (int c = 0; c < nC; ++c) {
+      const float4 r1 = sRec[team][c][1];
+      const int4 cn = sConn[team][c];
       const int ncf = cn.w >> 9;
       float old[GPL];
       vload<GPL>(out + (size_t)(c0 + c) * G, old);
       const float aez[3] = {r1.x, r1.y, r1.z};
-#pragma unroll
       for (int cf = 0; cf < 3; ++cf)
         if (cf < ncf && aez[cf] > 0.f) {
           const int cez = (cn.w >> (3 * cf)) & 7;
@@ -208,10 +240,10 @@ __global__ void __launch_bounds__(128) k_sweep32(Sweep32P p, int stage) {
           vstore<GPL>(sS + cez * G + g0, t);
         }
     }
-    for (int c = 0; c < nCorner; ++c) {
-      const float4 r0 = p.rec[(abase + c0 + c) * 2 + 0];
-      const float4 r1 = p.rec[(abase + c0 + c) * 2 + 1];
-      const int4 cn = p.conn[c0 + c];
+    for (int c = 0; c < nC; ++c) {
+      const float4 r0 = sRec[team][c][0];
+      const float4 r1 = sRec[team][c][1];
+      const int4 cn = sConn[team][c];
       const int ncf = cn.w >> 9;
       float s[GPL], v[GPL];
       vload<GPL>(sS + c * G + g0, s);
@@ -220,10 +252,8 @@ __global__ void __launch_bounds__(128) k_sweep32(Sweep32P p, int stage) {
       vstore<GPL>(out + (size_t)(c0 + c) * G, v);
       const float afp[3] = {r0.x, r0.y, r0.z};
       const int cfp[3] = {cn.x, cn.y, cn.z};
-#pragma unroll
       for (int cf = 0; cf < 3; ++cf)
-        if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f)
-          vstore<GPL>(p.psiB + ((size_t)a * p.nb + (size_t)(-cfp[cf] - 1)) * G + g0, v);
+        if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f) vstore<GPL>(outB + (size_t)(-cfp[cf] - 1) * G, v);
     }
   }
 }
@@ -276,6 +306,12 @@ int prepare_sweep32(Ctx &c) {
     if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
       return set_error(-7, "allocation of the FP32 corner records failed");
   }
+#define UMT_ATTR32(gt, gpl) \
+  cudaFuncSetAttribute(k_sweep32<gt, gpl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  UMT_ATTR32(1, 1) UMT_ATTR32(1, 2) UMT_ATTR32(1, 4) UMT_ATTR32(2, 1) UMT_ATTR32(2, 2) UMT_ATTR32(2, 4)
+  UMT_ATTR32(4, 1) UMT_ATTR32(4, 2) UMT_ATTR32(4, 4) UMT_ATTR32(8, 1) UMT_ATTR32(8, 2) UMT_ATTR32(8, 4)
+  UMT_ATTR32(16, 1) UMT_ATTR32(16, 2) UMT_ATTR32(16, 4) UMT_ATTR32(32, 1) UMT_ATTR32(32, 2) UMT_ATTR32(32, 4)
+#undef UMT_ATTR32
   const size_t n = (size_t)c.A * c.nc;
   k_corner_rec<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
       c.A, c.nc, c.nCFaces, c.afp64, c.aez64, c.Volume, (float4 *)c.rec32);
@@ -293,7 +329,8 @@ bool sweep32_supported(int G, int GT, int GPL) {
 
 void default_tile(int G, int *GT, int *GPL) {
   *GT = 0; *GPL = 0;
-  for (int gpl = 4; gpl >= 1; gpl /= 2)
+  const int pref[3] = {2, 1, 4};        // register use: GPL=2 ~124, GPL=1 ~96, GPL=4 ~200 per thread
+  for (int gpl : pref)
     if (G % gpl == 0 && sweep32_supported(G, G / gpl, gpl)) { *GT = G / gpl; *GPL = gpl; return; }
 }
 
@@ -305,20 +342,15 @@ static int team_stride(int G) {
 int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   Sweep32P p;
   p.nz = c.nz; p.nc = c.nc; p.nb = c.nb; p.A = c.A; p.G = c.G; p.stride = team_stride(c.G);
-  p.items = c.sch.items; p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
-  p.order = c.sch.order; p.numCorner = c.numCorner; p.cOffSet = c.cOffSet;
-  p.rec = (const float4 *)c.rec32; p.conn = (const int4 *)c.conn32; p.vol = c.vol32;
+  p.items2 = c.sch.items2; p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
+  p.order = c.sch.order;
+  p.rec = (const float4 *)c.rec32; p.conn = (const int4 *)c.conn32;
   p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
   const int TEAMS = 128 / GT;
   const size_t smem = (size_t)2 * TEAMS * p.stride * sizeof(float);
 #define UMT_LAUNCH32(gt, gpl)                                                                      \
   if (GT == gt && GPL == gpl) {                                                                    \
-    static bool attr = false;                                                                      \
-    if (!attr) {                                                                                   \
-      cudaFuncSetAttribute(k_sweep32<gt, gpl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); \
-      attr = true;                                                                                 \
-    }                                                                                              \
     for (int s = 0; s < c.sch.nStages; ++s) {                                                      \
       const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                    \
       k_sweep32<gt, gpl><<<blocks, 128, smem, c.stream>>>(p, s);                                   \

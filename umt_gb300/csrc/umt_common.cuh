@@ -25,6 +25,7 @@ namespace umt {
 // (direction, zone) whose longest upstream chain has h zones.
 struct Schedule {
   uint32_t *items = nullptr;      // [A*nz] bit31 = lagged (bad) zone, low bits a*nz+z
+  uint2 *items2 = nullptr;        // [A*nz] {items, cOffSet | numCorner << 28}
   int *stageCount = nullptr;      // [nz+2]
   int *stageOffset = nullptr;     // [nz+2]
   int *need = nullptr;            // [A*nz]
@@ -83,7 +84,8 @@ struct Ctx {
   double *scratch = nullptr;                    // reductions
   size_t scratchBytes = 0;
   // captured sweep graphs per precision
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][cur]
+  bool useGraphs = true;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evMid = nullptr;
   float lastMs = -1.f, lastKernMs = -1.f, lastTallyMs = -1.f;
   int launchesPerSweep[2] = {0, 0};
@@ -111,6 +113,8 @@ int build_schedule(Ctx &c);
 int capture_sweep_graph(Ctx &c, int precision);
 int launch_sweep_once(Ctx &c, int precision, bool tally);
 int launch_tally(Ctx &c, int precision);
+void invalidate_graphs(Ctx &c);
+int record_mid(Ctx &c);
 int launch_convert_source(Ctx &c);
 // source iteration and edits (si.cu)
 int launch_build_source(Ctx &c, const double *q);
