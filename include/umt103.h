@@ -138,6 +138,7 @@ typedef struct UmtSIResult {
   int sweeps;
   double rel_change;       /* last relative change of phi                   */
   double seconds;          /* device time                                   */
+  int grey_sweeps;         /* GTA grey S2 sweeps performed                  */
 } UmtSIResult;
 
 int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);
@@ -185,6 +186,13 @@ int umt103_last_timing(double *out3);
  * counterpart: the reference kernel fixes 4 groups x 32 zones per block
  * (gpu/GPU_SweepUCBxyz.cu:30-31). */
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane);
+
+/* FP32 sweep scheduling: 0 = one kernel launch per dependency stage (the
+ * hyperplane loop of snac/SweepUCBxyz.F90:103, all directions at once);
+ * 1 = one persistent launch in which each (direction, zone) pair
+ * starts as soon as its upwind zones have finished (bounded waits; a wait that
+ * gives up makes the sweep return UMT_ERR_TIMEOUT). */
+int umt103_set_sweep_mode(int mode);
 
 /* Number of kernels one sweep of the given precision launches (>= 0). */
 int umt103_launches_per_sweep(int precision);

@@ -97,3 +97,21 @@ def test_fp32_group_tiles(umtlib, G, tile):
     assert rel_err(Phi, ref["Phi"]) < 1e-5
     assert rel_err(Psi, ref["Psi"]) < 1e-4
     assert rel_err(PsiB, ref["PsiB"]) < 1e-4
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_fp32_sweep_modes(umtlib, mode):
+    """Per-stage launches (0) and the persistent dependency-driven launch (1)."""
+    prob = synthetic_problem((3, 2, 2), 4, 4, 16, seed=6, time_dependent=True)
+    m = prob.mesh
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    ref = oracle_sweep(prob, STotal=STotal, Psi=prob.psi0)
+    umtlib.init(m, prob.omega, prob.weight, prob.ngr)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    umtlib.set_sweep_mode(mode)
+    for _ in range(3):                       # repeated sweeps reuse the captured graph
+        PsiB = np.zeros((len(prob.weight), m.nbelem, prob.ngr))
+        Phi = umtlib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=capi.UMT_FP32)
+        assert rel_err(Phi, ref["Phi"]) < 1e-5
+        assert rel_err(PsiB, ref["PsiB"]) < 1e-4

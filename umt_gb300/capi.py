@@ -44,7 +44,7 @@ class UmtSIParams(C.Structure):
 
 class UmtSIResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("sweeps", C.c_int), ("rel_change", C.c_double),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("grey_sweeps", C.c_int)]
 
 
 class UmtEnergyTally(C.Structure):
@@ -77,7 +77,7 @@ def load():
                   "umt103_get_phi", "umt103_source_iterate", "umt103_tally",
                   "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry",
                   "umt103_last_timing", "umt103_launches_per_sweep", "umt103_select_device",
-                  "umt103_set_group_tile", "umt103_tally_precision"):
+                  "umt103_set_group_tile", "umt103_tally_precision", "umt103_set_sweep_mode"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
@@ -90,7 +90,8 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_get_phi", "umt103_source_iterate", "umt103_tally", "umt103_schedule_info",
             "umt103_get_schedule", "umt103_get_geometry", "umt103_last_sweep_ms",
             "umt103_error_string", "umt103_last_timing", "umt103_launches_per_sweep",
-            "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision"]
+            "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision",
+            "umt103_set_sweep_mode"]
 
 
 def check(rc):
@@ -208,7 +209,7 @@ class Library:
         if rc != 0 and not (allow_notconv and rc == -8):
             check(rc)
         return dict(iterations=res.iterations, sweeps=res.sweeps, rel_change=res.rel_change,
-                    seconds=res.seconds, converged=(rc == 0))
+                    seconds=res.seconds, converged=(rc == 0), grey_sweeps=res.grey_sweeps)
 
     def tally(self, siga=None, speed_light=299.792458, precision=None):
         siga = _c(siga, np.float64)
@@ -222,6 +223,9 @@ class Library:
 
     def set_group_tile(self, lanes_per_zone, groups_per_lane):
         check(self.lib.umt103_set_group_tile(int(lanes_per_zone), int(groups_per_lane)))
+
+    def set_sweep_mode(self, mode):
+        check(self.lib.umt103_set_sweep_mode(int(mode)))
 
     def select_device(self, device):
         check(self.lib.umt103_select_device(int(device)))

@@ -39,22 +39,34 @@ static void dfree(T *&p) {
   p = nullptr;
 }
 
+static void free_ctx(Ctx &c);
+
 static void free_all() {
-  Ctx &c = g;
+  if (g.gta) {
+    free_ctx(*g.gta);
+    delete g.gta;
+    g.gta = nullptr;
+  }
+  free_ctx(g);
+}
+
+static void free_ctx(Ctx &c) {
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j)
       if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
   dfree(c.numCorner); dfree(c.cOffSet); dfree(c.zoneFaces); dfree(c.zoneOpp); dfree(c.faceOpp);
   dfree(c.nCFaces); dfree(c.cFP); dfree(c.cEZ); dfree(c.CToFace); dfree(c.bdyToC); dfree(c.cToZone);
   dfree(c.px); dfree(c.A_fp); dfree(c.A_ez); dfree(c.Volume); dfree(c.VolumeZone); dfree(c.A_bdy);
-  dfree(c.Afp_raw); dfree(c.omega); dfree(c.weight);
+  dfree(c.Afp_raw); dfree(c.omega); dfree(c.weight); dfree(c.weight32);
   dfree(c.afp64); dfree(c.aez64); dfree(c.afp32); dfree(c.aez32);
   dfree(c.rec32); dfree(c.conn32); dfree(c.vol32);
   Schedule &s = c.sch;
   dfree(s.items); dfree(s.items2); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
+  dfree(s.needInit); dfree(c.dep); dfree(c.ticket);
   dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red);
+  dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch);
   if (c.ev0) cudaEventDestroy(c.ev0);
@@ -86,8 +98,36 @@ const char *umt103_error_string(void) { return g_err.c_str(); }
 
 void umt103_finalize(void) { free_all(); }
 
+static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags);
+
 int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   free_all();
+  int rc = init_ctx(g, m, q, ngr, flags);
+  if (rc) return rc;
+  // The grey (GTA) problem: same mesh, level-symmetric S2 (8 directions,
+  // |mu| = |eta| = |xi| = 1/sqrt(3), equal weights summing to 4 pi), one group,
+  // FP64 (the reference's gtaorder = 2, test_driver.cc:1206).
+  if (!(flags & 8)) {
+    const double s = 0.57735026918962576451, w = 4.0 * 3.14159265358979323846 / 8.0;
+    const double sg[8][3] = {{1, 1, 1}, {-1, 1, 1}, {-1, -1, 1}, {1, -1, 1},
+                             {1, 1, -1}, {-1, 1, -1}, {-1, -1, -1}, {1, -1, -1}};
+    double om[24], wt[8];
+    for (int a = 0; a < 8; ++a) {
+      for (int d = 0; d < 3; ++d) om[3 * a + d] = sg[a][d] * s;
+      wt[a] = w;
+    }
+    UmtQuad q2{8, om, wt};
+    g.gta = new Ctx();
+    rc = init_ctx(*g.gta, m, &q2, 1, 1);
+    if (rc) {
+      free_all();
+      return rc;
+    }
+  }
+  return 0;
+}
+
+static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   if (!m || !q || ngr <= 0 || q->nangles <= 0 || !q->omega || !q->weight)
     return set_error(UMT_ERR_ARG, "umt103_init: null mesh/quadrature or bad sizes");
   if (m->maxcf > UMT_MAXCF || m->maxFaces > UMT_MAXFACES || m->maxcf <= 0)
@@ -109,8 +149,7 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
     if (m->cOffSet[z] < 0 || m->cOffSet[z] + m->numCorner[z] > nc)
       return set_error(UMT_ERR_ARG, "zone %d corner range out of bounds", z);
   }
-  Ctx &c = g;
-  c.nz = nz; c.nc = nc; c.nb = nb; c.A = A; c.G = G; c.flags = flags ? flags : 3;
+  c.nz = nz; c.nc = nc; c.nb = nb; c.A = A; c.G = G; c.flags = (flags & 3) ? (flags & 3) : 3;
   UMT_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
   UMT_CUDA(cudaEventCreate(&c.ev0));
   UMT_CUDA(cudaEventCreate(&c.ev1));
@@ -205,6 +244,11 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   TRY(dalloc(&c.omega, 3 * (size_t)A)); TRY(dalloc(&c.weight, A));
   UMT_CUDA(cudaMemcpy(c.omega, q->omega, 3 * (size_t)A * sizeof(double), cudaMemcpyHostToDevice));
   UMT_CUDA(cudaMemcpy(c.weight, q->weight, (size_t)A * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    std::vector<float> w32(q->weight, q->weight + A);
+    TRY(dalloc(&c.weight32, A));
+    UMT_CUDA(cudaMemcpy(c.weight32, w32.data(), (size_t)A * sizeof(float), cudaMemcpyHostToDevice));
+  }
 
   // ---- projections (FP64 always: the schedule is decided in FP64) ----
   const size_t nP = (size_t)A * nc * UMT_MAXCF;
@@ -217,6 +261,7 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   const size_t nAZ = (size_t)A * nz;
   TRY(dalloc(&s.items, nAZ)); TRY(dalloc(&s.items2, nAZ)); TRY(dalloc(&s.stageCount, nz + 2)); TRY(dalloc(&s.stageOffset, nz + 2));
   TRY(dalloc(&s.need, nAZ)); TRY(dalloc(&s.exitMask, (nAZ + 3) & ~(size_t)3)); TRY(dalloc(&s.bad, nAZ));
+  TRY(dalloc(&s.needInit, nAZ)); TRY(dalloc(&c.dep, nAZ)); TRY(dalloc(&c.ticket, 1));
   TRY(dalloc(&s.order, nAZ)); TRY(dalloc(&s.level, nAZ)); TRY(dalloc(&s.nHyper, A));
   TRY(dalloc(&s.processed, 1));
   TRY(build_schedule(c));
@@ -402,6 +447,15 @@ int umt103_launches_per_sweep(int precision) {
   return g.launchesPerSweep[precision];
 }
 
+int umt103_set_sweep_mode(int mode) {
+  Ctx &c = g;
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (mode != 0 && mode != 1) return set_error(UMT_ERR_ARG, "sweep mode must be 0 or 1");
+  if (c.sweepMode != mode) invalidate_graphs(c);
+  c.sweepMode = mode;
+  return 0;
+}
+
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane) {
   Ctx &c = g;
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
@@ -450,13 +504,77 @@ int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume) {
   return 0;
 }
 
+// BiCGStab solve of the grey correction (rt/GTASolver.F90:219-402 structure:
+// two grey sweeps per iteration) followed by phi_g += chi_g eps.  Vectors are
+// FP64 on the device; slots of c.gtaVec: 0 x, 1 r, 2 rhat, 3 p, 4 v, 5 s, 6 t, 7 R.
+static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps) {
+  Ctx &q = *c.gta;
+  const int n = c.nc;
+  double *V = c.gtaVec;
+  double *x = V, *r = V + (size_t)n, *rh = V + 2 * (size_t)n, *p = V + 3 * (size_t)n, *v = V + 4 * (size_t)n,
+         *s = V + 5 * (size_t)n, *t = V + 6 * (size_t)n;
+  TRY(gta_prepare(c));
+  // A y = y - K y, with K y = one grey sweep of the source wtiso*sigma_s,grey*y
+  auto applyA = [&](const double *y, double *out) -> int {
+    TRY(gta_apply(c, y, 0.0));
+    ++*greySweeps;
+    return gta_axpbypcz(c, n, 1.0, y, 0.0, out, -1.0, q.Phi);
+  };
+  TRY(gta_apply(c, nullptr, 1.0));                 // b = K0 R
+  ++*greySweeps;
+  UMT_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, c.stream));
+  UMT_CUDA(cudaMemsetAsync(p, 0, (size_t)n * 8, c.stream));
+  UMT_CUDA(cudaMemsetAsync(v, 0, (size_t)n * 8, c.stream));
+  UMT_CUDA(cudaMemcpyAsync(r, q.Phi, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
+  UMT_CUDA(cudaMemcpyAsync(rh, q.Phi, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
+  double h[2];
+  TRY(gta_dot2(c, n, r, r, nullptr, nullptr, h));
+  const double bnorm = std::sqrt(h[0]);
+  if (!(bnorm > 0.0)) return 0;
+  double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+  for (int it = 0; it < maxit; ++it) {
+    TRY(gta_dot2(c, n, rh, r, nullptr, nullptr, h));
+    const double rho = h[0];
+    if (std::fabs(rho) < 1e-300) break;
+    const double beta = (rho / rho_old) * (alpha / omega);
+    TRY(gta_axpbypcz(c, n, 1.0, r, beta, p, -beta * omega, v));       // p = r + beta (p - omega v)
+    TRY(applyA(p, v));
+    TRY(gta_dot2(c, n, rh, v, nullptr, nullptr, h));
+    if (std::fabs(h[0]) < 1e-300) break;
+    alpha = rho / h[0];
+    TRY(gta_axpbypcz(c, n, 1.0, r, 0.0, s, -alpha, v));              // s = r - alpha v
+    TRY(applyA(s, t));
+    TRY(gta_dot2(c, n, t, s, t, t, h));
+    if (!(h[1] > 0.0)) {
+      TRY(gta_axpbypcz(c, n, alpha, p, 1.0, x, 0.0, nullptr));
+      break;
+    }
+    omega = h[0] / h[1];
+    TRY(gta_axpbypcz(c, n, alpha, p, 1.0, x, omega, s));              // x += alpha p + omega s
+    TRY(gta_axpbypcz(c, n, 1.0, s, 0.0, r, -omega, t));               // r = s - omega t
+    rho_old = rho;
+    TRY(gta_dot2(c, n, r, r, nullptr, nullptr, h));
+    if (std::sqrt(h[0]) < tol * bnorm || omega == 0.0) break;
+  }
+  return gta_correct(c, x);
+}
+
 int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   Ctx &c = g;
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (!prm || !res) return set_error(UMT_ERR_ARG, "null params/result");
   const int prec = prm->precision;
   if (prec != UMT_FP64 && prec != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
-  if (prm->use_gta) return set_error(UMT_ERR_ARG, "use_gta: call umt103_source_iterate_gta");
+  if (prm->use_gta && !c.gta) return set_error(UMT_ERR_STATE, "GTA context not created (init flag 8 set)");
+  if (prm->use_gta) {
+    if (!c.gtaChi) TRY(dalloc(&c.gtaChi, (size_t)c.nz * c.G));
+    if (!c.gtaVec) {
+      TRY(dalloc(&c.gtaVec, 8 * (size_t)c.nc));
+      UMT_CUDA(cudaMemset(c.gtaVec, 0, 8 * (size_t)c.nc * 8));
+    }
+    if (!c.gtaSigS) TRY(dalloc(&c.gtaSigS, c.nz));
+  }
+  int greySweeps = 0;
   const size_t ncG = (size_t)c.nc * c.G, nzG = (size_t)c.nz * c.G;
   if (!c.PhiPrev) TRY(dalloc(&c.PhiPrev, ncG));
   if (!c.red) TRY(dalloc(&c.red, 8));
@@ -479,6 +597,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
     TRY(launch_build_source(c, q));
     TRY(launch_sweep_once(c, prec, true));
     ++sweeps;
+    if (prm->use_gta) TRY(gta_solve(c, 10, 1.0e-4, &greySweeps));
     TRY(launch_change_norm(c, c.PhiPrev, c.red));
     double h[2];
     UMT_CUDA(cudaMemcpyAsync(h, c.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -498,6 +617,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   cudaEventElapsedTime(&ms, t0, t1);
   cudaEventDestroy(t0); cudaEventDestroy(t1);
   res->iterations = it; res->sweeps = sweeps; res->rel_change = rel; res->seconds = ms * 1e-3;
+  res->grey_sweeps = greySweeps;
   return conv ? 0 : set_error(UMT_ERR_NOTCONV, "not converged after %d iterations (rel change %.3e)", it, rel);
 }
 

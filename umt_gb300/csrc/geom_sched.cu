@@ -357,6 +357,7 @@ int build_schedule(Ctx &c) {
               c.nCFaces, c.cEZ, c.CToFace, c.afp64, c.aez64, s.need, s.exitMask, s.bad, s.order, c.status};
   const int B = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
   k_need<<<B, 256, 0, c.stream>>>(p);
+  UMT_CUDA(cudaMemcpyAsync(s.needInit, s.need, n * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
   k_corner_order<<<B, 256, 0, c.stream>>>(p);
   k_seed<<<B, 256, 0, c.stream>>>(c.nz, c.A, s.need, s.bad, s.items, s.stageCount, s.level, s.processed);
   UMT_CUDA(cudaGetLastError());

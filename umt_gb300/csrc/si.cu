@@ -13,6 +13,7 @@
 namespace umt {
 
 constexpr double WTISO = 0.079577471545947667884;   // 1/(4 pi), mods/Size_mod.F90:281
+#define TRY_SI(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
 
 __global__ void k_build_source(int nc, int G, const int *cToZone, const double *sigs,
                                const double *q, const double *Phi, double *STotal) {
@@ -92,6 +93,161 @@ __global__ void k_energy(int nc, int nb, int A, int G, const int *cToZone, const
     }
   }
   block_reduce_add<4>(v, out);
+}
+
+// ---------------------------------------------------------------------------
+// Grey transport acceleration (GTA).  After a multigroup sweep the change of
+// the scalar flux leaves a scattering residual R = sum_g sigma_s,g (phi_g -
+// phi_g_prev) (getCollisionRate, rt/getCollisionRate.F90:64-87).  The error it
+// drives is estimated by one grey S2 transport problem on the same mesh,
+//   Omega.grad(psi) + sigma_t,grey psi = (sigma_s,grey phi + R) / (4 pi),
+// solved by BiCGStab on (I - K) eps = K0 R with K = one grey sweep of the
+// scattering source (rt/GTASolver.F90:219-402), and added back as
+// phi_g += chi_g eps (rt/addGreyCorrections.F90:85).  Grey cross sections are
+// spectrum-weighted harmonic means (setGTAOpacity, rt/setGTAOpacity.F90:
+// 176-205, with no material coupling).  The spectrum chi that the
+// reference takes from its (absent) material-coupling solver is defined here
+// per zone as the shape of the current residual, |sigma_s,g dphi_g| summed
+// over the zone's corners and normalised.
+// ---------------------------------------------------------------------------
+__global__ void k_gta_spectrum(int nz, int G, double tau, const int *numCorner, const int *cOffSet,
+                               const double *Volume, const double *Sigt, const double *SigS, const double *Phi,
+                               const double *Prev, double *chi, double *greySigt, double *greySigs) {
+  for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const int c0 = cOffSet[z], nC = numCorner[z];
+    double rsum = 0.0;
+    for (int g = 0; g < G; ++g) {
+      double r = 0.0;
+      for (int k = 0; k < nC; ++k) {
+        const size_t e = (size_t)(c0 + k) * G + g;
+        r += Volume[c0 + k] * fabs(SigS[(size_t)z * G + g] * (Phi[e] - Prev[e]));
+      }
+      chi[(size_t)z * G + g] = r;
+      rsum += r;
+    }
+    double inv = 0.0, inv2 = 0.0, aav = 0.0;
+    for (int g = 0; g < G; ++g) {
+      const double x = rsum > 0.0 ? chi[(size_t)z * G + g] / rsum : 1.0 / G;
+      const double st = Sigt[(size_t)z * G + g];
+      const double si = 1.0 / st;
+      const double sa = st - SigS[(size_t)z * G + g] - tau;
+      inv += x * si;
+      inv2 += x * si * si;
+      aav += x * sa * si;
+      chi[(size_t)z * G + g] = x * si;
+    }
+    double gt, gs;
+    if (inv > 0.0) {
+      for (int g = 0; g < G; ++g) chi[(size_t)z * G + g] /= inv;
+      gt = inv / inv2;
+      const double ga = tau + aav / inv;
+      gs = gt - ga;
+      if (gs / gt <= 1.0e-10) { gs = 0.0; gt = ga; }
+    } else {
+      gt = tau > 0.0 ? tau : 1.0;
+      gs = 0.0;
+    }
+    greySigt[z] = gt;
+    greySigs[z] = gs;
+  }
+}
+
+// R(c) = sum_g sigma_s,g (phi_g - prev_g)
+__global__ void k_gta_residual(int nc, int G, const int *cToZone, const double *SigS, const double *Phi,
+                               const double *Prev, double *R) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int z = cToZone[c];
+    double s = 0.0;
+    for (int g = 0; g < G; ++g) {
+      const size_t e = (size_t)c * G + g;
+      s += SigS[(size_t)z * G + g] * (Phi[e] - Prev[e]);
+    }
+    R[c] = s;
+  }
+}
+
+// grey source: STotal(c) = wtiso (sigma_s,grey x(c) + wR R(c))
+__global__ void k_gta_source(int nc, const int *cToZone, const double *greySigs, const double *x, const double *R,
+                             double wR, double *STotal) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const double sx = x ? greySigs[cToZone[c]] * x[c] : 0.0;
+    STotal[c] = WTISO * (sx + wR * R[c]);
+  }
+}
+
+// y = a*x + b*y + c*z (any pointer may alias y; z may be null)
+__global__ void k_axpbypcz(int n, double a, const double *x, double b, double *y, double c, const double *z) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double v = a * x[i];
+    if (b != 0.0) v += b * y[i];
+    if (z) v += c * z[i];
+    y[i] = v;
+  }
+}
+
+__global__ void k_dot2(int n, const double *x, const double *y, const double *u, const double *w, double *out2) {
+  double v[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    v[0] += x[i] * y[i];
+    if (u) v[1] += u[i] * w[i];
+  }
+  block_reduce_add<2>(v, out2);
+}
+
+// phi_g(c) += chi_g(zone) eps(c)
+__global__ void k_gta_correct(int nc, int G, const int *cToZone, const double *chi, const double *eps, double *Phi) {
+  const size_t n = (size_t)nc * G;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i / G), g = (int)(i - (size_t)c * G);
+    Phi[i] += chi[(size_t)cToZone[c] * G + g] * eps[c];
+  }
+}
+
+int gta_prepare(Ctx &c) {
+  Ctx &q = *c.gta;
+  const int B = 152 * 4;
+  k_gta_spectrum<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, c.G, c.tau, c.numCorner, c.cOffSet, c.Volume,
+                                                          c.Sigt, c.SigS, c.Phi, c.PhiPrev, c.gtaChi, q.Sigt,
+                                                          c.gtaSigS);
+  UMT_CUDA(cudaMemcpyAsync(q.SigS, c.gtaSigS, c.nz * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  // R lives in slot 7 of the BiCGStab vectors
+  k_gta_residual<<<B, 256, 0, c.stream>>>(c.nc, c.G, c.cToZone, c.SigS, c.Phi, c.PhiPrev, c.gtaVec + 7 * (size_t)c.nc);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// y <- K x + wR * K0 R  (one grey sweep; result is the grey context's Phi)
+int gta_apply(Ctx &c, const double *x, double wR) {
+  Ctx &q = *c.gta;
+  k_gta_source<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.cToZone, c.gtaSigS, x, c.gtaVec + 7 * (size_t)c.nc, wR,
+                                              q.STotal);
+  UMT_CUDA(cudaGetLastError());
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  TRY_SI(launch_sweep_once(q, 0, true));
+  UMT_CUDA(cudaStreamSynchronize(q.stream));
+  return 0;
+}
+
+int gta_axpbypcz(Ctx &c, int n, double a, const double *x, double b, double *y, double cc, const double *z) {
+  k_axpbypcz<<<152 * 4, 256, 0, c.stream>>>(n, a, x, b, y, cc, z);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int gta_dot2(Ctx &c, int n, const double *x, const double *y, const double *u, const double *w, double *h2) {
+  UMT_CUDA(cudaMemsetAsync(c.red + 4, 0, 2 * sizeof(double), c.stream));
+  k_dot2<<<152 * 4, 256, 0, c.stream>>>(n, x, y, u, w, c.red + 4);
+  UMT_CUDA(cudaMemcpyAsync(h2, c.red + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int gta_correct(Ctx &c, const double *eps) {
+  const size_t n = (size_t)c.nc * c.G;
+  k_gta_correct<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, c.stream>>>(c.nc, c.G, c.cToZone,
+                                                                                       c.gtaChi, eps, c.Phi);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
 }
 
 int launch_build_source(Ctx &c, const double *q) {

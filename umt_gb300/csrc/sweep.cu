@@ -198,9 +198,39 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
 
 // psi -> phi tally: PhiTotal(g,c) = sum_a w_a psi_a(g,c), accumulated in FP64
 // (control/getPhiTotal_OMPOL.F90:63-131 does the same per direction).
-// Each thread owns 4 consecutive (corner, group) entries and walks the
-// directions with 4 independent partial sums, so many 128-bit loads are in
-// flight per thread (the pass is bound by reading psi once).
+// FP32 angular flux: each thread owns 4 consecutive (corner, group) entries;
+// products w_a*psi_a of one block of 8 directions are summed in FP32 and the
+// block sums are accumulated in FP64.  GB300's FP64 rate is 1/64 of FP32, so
+// an FP64 multiply-add per (direction, entry) would make this HBM pass
+// FP64-bound; one FP64 add per 8 directions keeps it at the read bandwidth.
+__global__ void __launch_bounds__(256) k_tally32(int A, size_t ncG, const float *w32, const float *psi, double *Phi) {
+  const size_t n4 = ncG / 4;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n4; q += (size_t)gridDim.x * blockDim.x) {
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int a0 = 0; a0 < A; a0 += 8) {
+      float s[4] = {0.f, 0.f, 0.f, 0.f};
+      const int a1 = min(A, a0 + 8);
+#pragma unroll 8
+      for (int a = a0; a < a1; ++a) {
+        const float w = w32[a];
+        const float4 v = *reinterpret_cast<const float4 *>(psi + (size_t)a * ncG + 4 * q);
+        s[0] = fmaf(w, v.x, s[0]); s[1] = fmaf(w, v.y, s[1]); s[2] = fmaf(w, v.z, s[2]); s[3] = fmaf(w, v.w, s[3]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[j] += (double)s[j];
+    }
+    *reinterpret_cast<double2 *>(Phi + 4 * q) = make_double2(acc[0], acc[1]);
+    *reinterpret_cast<double2 *>(Phi + 4 * q + 2) = make_double2(acc[2], acc[3]);
+  }
+  for (size_t e = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncG; e += (size_t)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int a = 0; a < A; ++a) t += (double)(w32[a] * psi[(size_t)a * ncG + e]);
+    Phi[e] = t;
+  }
+}
+
+// FP64 angular flux (parity path): FP64 products and sums; each thread owns 4
+// consecutive entries and walks the directions with 4 independent partial sums.
 template <typename T>
 __global__ void __launch_bounds__(256) k_tally(int A, size_t ncG, const double *weight, const T *psi, double *Phi) {
   const size_t n4 = ncG / 4;
@@ -301,8 +331,11 @@ static int enqueue_sweep(Ctx &c, int cur) {
   }
   TRY_RC(record_mid(c));
   const size_t ncG = (size_t)c.nc * c.G;
-  k_tally<T><<<(int)std::min<size_t>((ncG + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
-      c.A, ncG, c.weight, (const T *)(sizeof(T) == 8 ? (const void *)c.psi64[1 - cur] : (const void *)c.psi32[1 - cur]), c.Phi);
+  const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
+  if constexpr (sizeof(T) == 4)
+    k_tally32<<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi);
+  else
+    k_tally<double><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight, c.psi64[1 - cur], c.Phi);
   UMT_CUDA(cudaGetLastError());
   return 0;
 }

@@ -64,21 +64,29 @@ __device__ __forceinline__ void vstore(float *p, const float (&v)[N]) {
 
 constexpr int SW32_NT = 128;
 
-template <int GT, int GPL>
-__global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
-  constexpr int TEAMS = SW32_NT / GT;
-  extern __shared__ float4 smem4[];
-  __shared__ float4 sRec[TEAMS][UMT_MAXCORNER][2];
-  __shared__ int4 sConn[TEAMS][UMT_MAXCORNER];
-  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
-  const int k = blockIdx.x * TEAMS + team;
-  if (k >= p.stageCount[stage]) return;            // whole teams leave together
-  const unsigned teammask = (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
+// Upwind fluxes written by other teams of the same launch (persistent mode)
+// are read through L2 only (ld.global.cg), never from a possibly stale L1 line.
+template <int N, bool COHERENT>
+__device__ __forceinline__ void vload_up(const float *p, float (&v)[N]) {
+  if constexpr (!COHERENT) {
+    vload<N>(p, v);
+  } else if constexpr (N == 1) {
+    v[0] = __ldcg(p);
+  } else if constexpr (N == 2) {
+    const float2 t = __ldcg(reinterpret_cast<const float2 *>(p));
+    v[0] = t.x; v[1] = t.y;
+  } else {
+    const float4 t = __ldcg(reinterpret_cast<const float4 *>(p));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+}
+
+// One (direction, zone) pair for the GT lanes of a team.  sRec/sConn are this
+// team's staging slots; sQ/sS its [8][G] source and running-source arrays.
+template <int GT, int GPL, bool COHERENT>
+__device__ __forceinline__ void sweep_zone(const Sweep32P &p, const uint2 w, const int lane, const unsigned teammask,
+                                           float *sQ, float *sS, float4 (*sRec)[2], int4 *sConn) {
   const int G = GT * GPL;
-  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.stride;   // [8][G]
-  float *sS = sQ + (size_t)TEAMS * p.stride;                                 // running source
-  // ---- round trip 1: the work item ----
-  const uint2 w = p.items2[p.stageOffset[stage] + k];
   const bool bad = (w.x >> 31) != 0;
   const uint32_t it = w.x & 0x7fffffffu;
   const int a = (int)(it / (uint32_t)p.nz);
@@ -88,8 +96,8 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
   const size_t abase = (size_t)a * p.nc;
   // ---- round trip 2: structure (cooperative), sources, cross sections ----
   for (int e = lane; e < 3 * nC; e += GT) {
-    if (e < 2 * nC) sRec[team][e >> 1][e & 1] = p.rec[(abase + c0) * 2 + e];
-    else sConn[team][e - 2 * nC] = p.conn[c0 + e - 2 * nC];
+    if (e < 2 * nC) sRec[e >> 1][e & 1] = p.rec[(abase + c0) * 2 + e];
+    else sConn[e - 2 * nC] = p.conn[c0 + e - 2 * nC];
   }
   float po[UMT_MAXCORNER][GPL], st[UMT_MAXCORNER][GPL];
 #pragma unroll
@@ -109,7 +117,7 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
 #pragma unroll
   for (int c = 0; c < UMT_MAXCORNER; ++c) {
     if (c < nC) {
-      const float v = sRec[team][c][1].w;
+      const float v = sRec[c][1].w;
       float q[GPL], s[GPL];
 #pragma unroll
       for (int j = 0; j < GPL; ++j) { q[j] = fmaf(p.tau, po[c][j], st[c][j]); s[j] = v * q[j]; }
@@ -121,8 +129,8 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
   float pf[UMT_MAXCORNER][3][GPL];
 #pragma unroll
   for (int c = 0; c < UMT_MAXCORNER; ++c) {
-    const float4 r0 = sRec[team][c][0];
-    const int4 cn = sConn[team][c];
+    const float4 r0 = sRec[c][0];
+    const int4 cn = sConn[c];
     const float afp[3] = {r0.x, r0.y, r0.z};
     const int cfp[3] = {cn.x, cn.y, cn.z};
     const int ncf = cn.w >> 9;
@@ -134,7 +142,7 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
         const int up = cfp[cf];
         const float *src_p = up >= 0 ? p.psi_new + (abase + up) * G + g0
                                      : p.psiB + ((size_t)a * p.nb + (size_t)(-up - 1)) * G + g0;
-        vload<GPL>(src_p, pf[c][cf]);
+        vload_up<GPL, COHERENT>(src_p, pf[c][cf]);
       }
     }
   }
@@ -142,9 +150,9 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
 #pragma unroll
   for (int c = 0; c < UMT_MAXCORNER; ++c) {
     if (c < nC) {
-      const float4 r0 = sRec[team][c][0];
-      const float4 r1 = sRec[team][c][1];
-      const int4 cn = sConn[team][c];
+      const float4 r0 = sRec[c][0];
+      const float4 r1 = sRec[c][1];
+      const int4 cn = sConn[c];
       const float afp[3] = {r0.x, r0.y, r0.z};
       const float aez[3] = {r1.x, r1.y, r1.z};
       const int meta = cn.w;
@@ -168,15 +176,20 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
           vload<GPL>(sS + cez * G + g0, sz);
           const int ifp = (cf + 1) % 3;
           if (ncf == 3 && afp[ifp] < 0.f) {
-            const float a2 = ae * ae;
+            // The reference's closure (SweepUCBxyz.F90:230-243) divided through by
+            // aez^4: with x = sigma*V/aez, gnum = aez^4*N(x), gden*sigma = aez^4*2x*Dh(x),
+            // N = 1.82x^2+4x+3, Dh = 2x^3+3x^2+2x+1, so
+            //   sez = V*(N*(sigma*psi_opp - Qc) + Dh*(Qc - Qz)) / (N + 2x*Dh).
+            // x is capped at 1e8 (sez ~ V*(Qc-Qz)/(2x) there) to stay finite in FP32.
+            const float rae = __frcp_rn(ae);
 #pragma unroll
             for (int j = 0; j < GPL; ++j) {
-              const float sigv = sig[j] * vol;
-              const float sigv2 = sigv * sigv;
-              const float gnum = a2 * (1.82f * sigv2 + ae * (4.f * sigv + 3.f * ae));
-              const float gden = vol * (4.f * sigv * sigv2 + ae * (6.f * sigv2 + 2.f * ae * (2.f * sigv + ae)));
-              const float num = vol * gnum * (sig[j] * pf[c][ifp][j] - Qc[j]) + 0.5f * ae * gden * (Qc[j] - Qz[j]);
-              sez[j] = __fdividef(num, gnum + gden * sig[j]);
+              const float x = fminf(sig[j] * vol * rae, 1.0e8f);
+              const float N = fmaf(fmaf(1.82f, x, 4.f), x, 3.f);
+              const float Dh = fmaf(fmaf(fmaf(2.f, x, 3.f), x, 2.f), x, 1.f);
+              const float den = fmaf(2.f * x, Dh, N);
+              const float num = fmaf(N, fmaf(sig[j], pf[c][ifp][j], -Qc[j]), Dh * (Qc[j] - Qz[j]));
+              sez[j] = vol * __fdividef(num, den);
             }
           } else {
 #pragma unroll
@@ -196,9 +209,9 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
   if (!bad) {
     for (int i = 0; i < nC; ++i) {
       const int c = (int)((ord >> (4 * i)) & 15u);
-      const float4 r0 = sRec[team][c][0];
-      const float4 r1 = sRec[team][c][1];
-      const int4 cn = sConn[team][c];
+      const float4 r0 = sRec[c][0];
+      const float4 r1 = sRec[c][1];
+      const int4 cn = sConn[c];
       const int ncf = cn.w >> 9;
       float s[GPL], v[GPL];
       vload<GPL>(sS + c * G + g0, s);
@@ -224,8 +237,8 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
   } else {
     // direct solve with the previous iterate of the zone's corners
     for (int c = 0; c < nC; ++c) {
-      const float4 r1 = sRec[team][c][1];
-      const int4 cn = sConn[team][c];
+      const float4 r1 = sRec[c][1];
+      const int4 cn = sConn[c];
       const int ncf = cn.w >> 9;
       float old[GPL];
       vload<GPL>(out + (size_t)(c0 + c) * G, old);
@@ -241,9 +254,9 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
         }
     }
     for (int c = 0; c < nC; ++c) {
-      const float4 r0 = sRec[team][c][0];
-      const float4 r1 = sRec[team][c][1];
-      const int4 cn = sConn[team][c];
+      const float4 r0 = sRec[c][0];
+      const float4 r1 = sRec[c][1];
+      const int4 cn = sConn[c];
       const int ncf = cn.w >> 9;
       float s[GPL], v[GPL];
       vload<GPL>(sS + c * G + g0, s);
@@ -255,6 +268,91 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
       for (int cf = 0; cf < 3; ++cf)
         if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f) vstore<GPL>(outB + (size_t)(-cfp[cf] - 1) * G, v);
     }
+  }
+}
+
+__device__ __forceinline__ unsigned team_mask(int GT, int tid) {
+  return (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
+}
+
+// Level-synchronous form: one launch per dependency stage; the stage's
+// (direction, zone) pairs are independent.
+template <int GT, int GPL>
+__global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
+  constexpr int TEAMS = SW32_NT / GT;
+  extern __shared__ float4 smem4[];
+  __shared__ float4 sRec[TEAMS][UMT_MAXCORNER][2];
+  __shared__ int4 sConn[TEAMS][UMT_MAXCORNER];
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const int k = blockIdx.x * TEAMS + team;
+  if (k >= p.stageCount[stage]) return;            // whole teams leave together
+  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.stride;
+  float *sS = sQ + (size_t)TEAMS * p.stride;
+  const uint2 w = p.items2[p.stageOffset[stage] + k];
+  sweep_zone<GT, GPL, false>(p, w, lane, team_mask(GT, tid), sQ, sS, sRec[team], sConn[team]);
+}
+
+// Persistent form: every team takes work items in dependency-stage order from
+// a global ticket, waits until all its upwind zones have signalled, sweeps the
+// zone and signals its downwind zones.  Items are taken in stage order, so the
+// earliest unfinished item never waits on anything unfinished: no deadlock, and
+// no block needs to be co-resident.  Waits are bounded: after kWaitLimit polls
+// the team records UMT_DEV_TIMEOUT in the status word and proceeds, so the
+// launch always ends and the host reports the error.
+constexpr long long kWaitLimit = 1ll << 22;   // ~0.5 s of polling
+
+struct PersistP {
+  int total;                      // A * nz items
+  int *ticket;                    // reset to 0 before the launch
+  int *dep;                       // per item: upwind zones not yet done
+  const uint8_t *exitMask;        // per item: exit faces
+  const int *zoneOpp, *zoneFaces;
+  unsigned int *status;
+};
+
+template <int GT, int GPL>
+__global__ void __launch_bounds__(SW32_NT) k_sweep32_persistent(Sweep32P p, PersistP q) {
+  constexpr int TEAMS = SW32_NT / GT;
+  extern __shared__ float4 smem4[];
+  __shared__ float4 sRec[TEAMS][UMT_MAXCORNER][2];
+  __shared__ int4 sConn[TEAMS][UMT_MAXCORNER];
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const unsigned tm = team_mask(GT, tid);
+  const int leader = (tid & 31) / GT * GT;       // lane id (in warp) of the team's first lane
+  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.stride;
+  float *sS = sQ + (size_t)TEAMS * p.stride;
+  while (true) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(q.ticket, 1);
+    t = __shfl_sync(tm, t, leader);
+    if (t >= q.total) break;
+    const uint2 w = p.items2[t];
+    const uint32_t it = w.x & 0x7fffffffu;
+    if (lane == 0) {
+      long long n = 0;
+      while (*((volatile int *)(q.dep + it)) > 0) {
+        if (++n > kWaitLimit) { atomicOr(q.status, UMT_DEV_TIMEOUT); break; }
+        // once any team has given up, nobody waits any more: the launch drains
+        if ((n & 1023) == 0 && (*((volatile unsigned *)q.status) & UMT_DEV_TIMEOUT)) break;
+        __nanosleep(32);
+      }
+      __threadfence();
+    }
+    __syncwarp(tm);
+    sweep_zone<GT, GPL, true>(p, w, lane, tm, sQ, sS, sRec[team], sConn[team]);
+    __threadfence();
+    __syncwarp(tm);
+    if (lane == 0) {
+      const int a = (int)(it / (uint32_t)p.nz);
+      const int z = (int)(it - (uint32_t)a * p.nz);
+      const uint8_t m = q.exitMask[it];
+      for (int f = 0; f < q.zoneFaces[z]; ++f)
+        if (m & (1u << f)) {
+          const int zo = q.zoneOpp[z * UMT_MAXFACES + f];
+          if (zo >= 0) atomicSub(q.dep + (size_t)a * p.nz + zo, 1);
+        }
+    }
+    __syncwarp(tm);
   }
 }
 
@@ -307,7 +405,8 @@ int prepare_sweep32(Ctx &c) {
       return set_error(-7, "allocation of the FP32 corner records failed");
   }
 #define UMT_ATTR32(gt, gpl) \
-  cudaFuncSetAttribute(k_sweep32<gt, gpl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  cudaFuncSetAttribute(k_sweep32<gt, gpl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024); \
+  cudaFuncSetAttribute(k_sweep32_persistent<gt, gpl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
   UMT_ATTR32(1, 1) UMT_ATTR32(1, 2) UMT_ATTR32(1, 4) UMT_ATTR32(2, 1) UMT_ATTR32(2, 2) UMT_ATTR32(2, 4)
   UMT_ATTR32(4, 1) UMT_ATTR32(4, 2) UMT_ATTR32(4, 4) UMT_ATTR32(8, 1) UMT_ATTR32(8, 2) UMT_ATTR32(8, 4)
   UMT_ATTR32(16, 1) UMT_ATTR32(16, 2) UMT_ATTR32(16, 4) UMT_ATTR32(32, 1) UMT_ATTR32(32, 2) UMT_ATTR32(32, 4)
@@ -349,11 +448,28 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
   const int TEAMS = 128 / GT;
   const size_t smem = (size_t)2 * TEAMS * p.stride * sizeof(float);
+  PersistP q;
+  q.total = c.A * c.nz; q.ticket = c.ticket; q.dep = c.dep; q.exitMask = c.sch.exitMask;
+  q.zoneOpp = c.zoneOpp; q.zoneFaces = c.zoneFaces; q.status = c.status;
+  if (c.sweepMode == 1) {
+    UMT_CUDA(cudaMemcpyAsync(c.dep, c.sch.needInit, (size_t)q.total * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
+    UMT_CUDA(cudaMemsetAsync(c.ticket, 0, sizeof(int), c.stream));
+  }
+  int dev = 0, nsm = 0;
+  UMT_CUDA(cudaGetDevice(&dev));
+  UMT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
 #define UMT_LAUNCH32(gt, gpl)                                                                      \
   if (GT == gt && GPL == gpl) {                                                                    \
-    for (int s = 0; s < c.sch.nStages; ++s) {                                                      \
-      const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                    \
-      k_sweep32<gt, gpl><<<blocks, 128, smem, c.stream>>>(p, s);                                   \
+    if (c.sweepMode == 1) {                                                                        \
+      int per = 0;                                                                                 \
+      UMT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sweep32_persistent<gt, gpl>, 128, smem)); \
+      const int blocks = std::max(1, std::min(per * nsm, (q.total + TEAMS - 1) / TEAMS));         \
+      k_sweep32_persistent<gt, gpl><<<blocks, 128, smem, c.stream>>>(p, q);                        \
+    } else {                                                                                       \
+      for (int s = 0; s < c.sch.nStages; ++s) {                                                    \
+        const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                  \
+        k_sweep32<gt, gpl><<<blocks, 128, smem, c.stream>>>(p, s);                                 \
+      }                                                                                            \
     }                                                                                              \
     UMT_CUDA(cudaGetLastError());                                                                  \
     return 0;                                                                                      \

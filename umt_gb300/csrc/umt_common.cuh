@@ -29,6 +29,7 @@ struct Schedule {
   int *stageCount = nullptr;      // [nz+2]
   int *stageOffset = nullptr;     // [nz+2]
   int *need = nullptr;            // [A*nz]
+  int *needInit = nullptr;        // [A*nz] upwind-zone counts before the stage build
   uint8_t *exitMask = nullptr;    // [A*nz] bit f: zone face f is an exit face
   uint8_t *bad = nullptr;         // [A*nz] intra-zone corner cycle
   uint32_t *order = nullptr;      // [A*nz] corner solve order, 8 nibbles
@@ -53,6 +54,7 @@ struct Ctx {
   double *px = nullptr, *A_fp = nullptr, *A_ez = nullptr, *Volume = nullptr;
   double *VolumeZone = nullptr, *A_bdy = nullptr, *Afp_raw = nullptr;
   double *omega = nullptr, *weight = nullptr;
+  float *weight32 = nullptr;
   std::vector<double> h_omega, h_weight;
   // per-direction corner-face projections Omega.A  [A][nc][3]
   double *afp64 = nullptr, *aez64 = nullptr;
@@ -63,6 +65,9 @@ struct Ctx {
   float *vol32 = nullptr;                       // [nc]
   bool rec32Ready = false;
   int tileGT = 0, tileGPL = 0;                  // FP32 group tile (0: choose)
+  int sweepMode = 0;                            // FP32: 0 = one launch per stage, 1 = persistent
+  int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
+  int *ticket = nullptr;                        // persistent-mode work ticket
   Schedule sch;
   // materials and sources
   double *Sigt = nullptr, *SigS = nullptr;      // [nz][G]
@@ -90,6 +95,11 @@ struct Ctx {
   float lastMs = -1.f, lastKernMs = -1.f, lastTallyMs = -1.f;
   int launchesPerSweep[2] = {0, 0};
   int sweepGT[2] = {0, 0};                      // group tile per precision
+  Ctx *gta = nullptr;                           // grey S2 problem on the same mesh (GTA)
+  // GTA work arrays (on the main context)
+  double *gtaChi = nullptr;                     // [nz][G] correction spectrum
+  double *gtaVec = nullptr;                     // [8][nc] BiCGStab vectors
+  double *gtaSigS = nullptr;                    // [nz] grey scattering (for inner products)
 };
 
 extern Ctx g;
@@ -120,6 +130,12 @@ int launch_convert_source(Ctx &c);
 int launch_build_source(Ctx &c, const double *q);
 int launch_change_norm(Ctx &c, double *prev, double *out2);
 int launch_energy(Ctx &c, const double *siga_dev, int precision, double *out4);
+// grey transport acceleration (si.cu)
+int gta_prepare(Ctx &c);
+int gta_apply(Ctx &c, const double *x, double wR);
+int gta_axpbypcz(Ctx &c, int n, double a, const double *x, double b, double *y, double cc, const double *z);
+int gta_dot2(Ctx &c, int n, const double *x, const double *y, const double *u, const double *w, double *h2);
+int gta_correct(Ctx &c, const double *eps);
 // production FP32 kernel (sweep32.cu)
 int prepare_sweep32(Ctx &c);
 bool sweep32_supported(int G, int GT, int GPL);
