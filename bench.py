@@ -191,6 +191,30 @@ def cpu_baseline_sample(prob, budget_s=20.0):
             "sample": f"{n_ang} of {len(prob.weight)} directions on the full mesh, all groups, FP64"}
 
 
+def time_to_converge(lib, prob, use_gta=False, tol64=1e-8, tol32=1e-7):
+    """Second half of the metric: wall time of source iteration to convergence,
+    plain FP64 GPU sweeps versus the FP32 sweep (FP64 tallies), and the FP32
+    solution's relative L2 error against the FP64 one.  The FP64 GPU path is
+    the reference here: it agrees with the CPU oracle to 1e-12 (tests)."""
+    from umt_gb300 import capi
+    m = prob.mesh
+    out = {}
+    for prec, tol in ((capi.UMT_FP64, tol64), (capi.UMT_FP32, tol32)):
+        lib.set_psi(prob.psi0, None)
+        t0 = time.perf_counter()
+        r = lib.source_iterate(precision=prec, rel_tol=tol, q_ext=prob.q_ext, save_psi=False, max_iters=400,
+                               use_gta=(use_gta and prec == capi.UMT_FP32), allow_notconv=True)
+        wall = time.perf_counter() - t0
+        out[prec] = (r, wall, lib.get_phi())
+    r64, w64, phi64 = out[capi.UMT_FP64]
+    r32, w32, phi32 = out[capi.UMT_FP32]
+    err = float(np.linalg.norm(phi32 - phi64) / np.linalg.norm(phi64))
+    return {"fp64_plain_s": w64, "fp64_iterations": r64["iterations"], "fp64_device_s": r64["seconds"],
+            "fp32_s": w32, "fp32_iterations": r32["iterations"], "fp32_device_s": r32["seconds"],
+            "fp32_gta": bool(use_gta), "speedup": w64 / w32, "rel_l2_err_fp32_vs_fp64": err,
+            "tolerance_fp64": tol64, "tolerance_fp32": tol32}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -200,6 +224,8 @@ def main():
     ap.add_argument("--tiles", type=int, default=20)
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
+    ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -222,7 +248,8 @@ def main():
     prob = make_problem(args.tiles)
     m = prob.mesh
     A, G = len(prob.weight), prob.ngr
-    lib.init(m, prob.omega, prob.weight, G, flags=2 if prec == capi.UMT_FP32 else 1)
+    lib.init(m, prob.omega, prob.weight, G, flags=3 if world == 1 and not args.no_ttc else
+             (2 if prec == capi.UMT_FP32 else 1))
     lib.set_materials(prob.sigt, prob.sigs, prob.tau)
     lib.set_psi(prob.psi0, None)
     STotal = np.ascontiguousarray(source_from_phi(prob, np.zeros((m.ncornr, G))))
@@ -299,6 +326,8 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
     }
+    if world == 1 and not args.no_ttc:
+        line["time_to_converge"] = time_to_converge(lib, prob, use_gta=args.gta)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_sample(prob)
     print(json.dumps(line), flush=True)

@@ -84,8 +84,28 @@ typedef struct UmtQuad {
  */
 int umt103_init(const UmtMesh *mesh, const UmtQuad *quad, int ngr, int flags);
 
-/* Release every device buffer (idempotent). */
+/* Release every device buffer of the current context (idempotent). */
 void umt103_finalize(void);
+
+/*
+ * Several independent problems can be resident at once.  Context 0 always
+ * exists; umt103_context_create adds one (empty until umt103_init), and every
+ * other entry point acts on the context made current by umt103_context_select.
+ * No reference counterpart: Teton keeps one problem in module state.
+ */
+int umt103_context_create(int *id);
+int umt103_context_select(int id);
+int umt103_context_current(void);
+int umt103_context_destroy(int id);   /* id > 0; releases its buffers */
+
+/*
+ * One sweep of each listed context from a single CUDA graph launch: the
+ * contexts' captured sweeps become independent child graphs, so problems of
+ * different zone, group and direction counts run concurrently.  *ms (may be
+ * NULL) receives the device time of the whole batch.  Each context's
+ * PhiTotal is left on its device (umt103_get_phi after selecting it).
+ */
+int umt103_batch_sweep(const int *ids, int n, int precision, double *ms);
 
 /*
  * Materials: sigt = total opacity including tau, Sigt(G,nzones) as
@@ -131,6 +151,7 @@ typedef struct UmtSIParams {
   int use_gta;             /* 1: grey transport acceleration after each sweep */
   const double *q_ext;     /* [nzones*G] isotropic external source, or NULL */
   int save_psi;            /* final savePsi sweep                           */
+  int warm_start;          /* 1: start from the current PhiTotal, 0: from zero */
 } UmtSIParams;
 
 typedef struct UmtSIResult {
@@ -142,6 +163,13 @@ typedef struct UmtSIResult {
 } UmtSIResult;
 
 int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);
+
+/* GTA options: BiCGStab iterations per correction (each costs two grey S2
+ * sweeps; the reference's default grey budget is 21 sweeps,
+ * mods/default_iter_controls_mod.F90:10-22), relative residual tolerance, and
+ * the correction spectrum (0: shape of the scattering residual, 1: residual
+ * weighted by 1/(1-c) per group). */
+int umt103_set_gta(int max_krylov, double tol, int spectrum);
 
 /*
  * Energy tallies of the last sweep (rtedit, aux/rtedit.F90:8-327, and
@@ -160,6 +188,7 @@ int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *tally);
 /* Same, on the angular flux of the given precision (UMT_FP64 / UMT_FP32). */
 int umt103_tally_precision(const double *siga, double speed_light, int precision,
                            UmtEnergyTally *tally);
+
 
 /* Schedule statistics for one direction. */
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);
@@ -187,8 +216,10 @@ int umt103_last_timing(double *out3);
  * (gpu/GPU_SweepUCBxyz.cu:30-31). */
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane);
 
-/* FP32 sweep scheduling: 0 = one kernel launch per dependency stage (the
- * hyperplane loop of snac/SweepUCBxyz.F90:103, all directions at once);
+/* FP32 sweep scheduling: 0 (default) = one kernel launch per dependency stage
+ * (the hyperplane loop of snac/SweepUCBxyz.F90:103, all directions at once),
+ * with the compact face-list kernel where the group tile allows it;
+ * 2 = one kernel launch per stage, unrolled corner-slot kernel;
  * 1 = one persistent launch in which each (direction, zone) pair
  * starts as soon as its upwind zones have finished (bounded waits; a wait that
  * gives up makes the sweep return UMT_ERR_TIMEOUT). */

@@ -115,3 +115,38 @@ def test_fp32_sweep_modes(umtlib, mode):
         Phi = umtlib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=capi.UMT_FP32)
         assert rel_err(Phi, ref["Phi"]) < 1e-5
         assert rel_err(PsiB, ref["PsiB"]) < 1e-4
+
+
+def test_batch_of_contexts_matches_single_runs(umtlib):
+    """Several problems of different size, group and direction counts resident
+    in separate contexts, swept from one graph launch, give each problem's
+    single-context result."""
+    from umt_gb300.problems import synthetic_problem as sp
+    specs = [((2, 2, 1), 2, 4, 31), ((3, 2, 1), 4, 8, 32), ((2, 3, 2), 2, 16, 33)]
+    probs = [sp(t, P, P, G, seed=s, time_dependent=True) for (t, P, G, s) in specs]
+    single = []
+    for pr in probs:
+        umtlib.init(pr.mesh, pr.omega, pr.weight, pr.ngr, flags=2 | 8)
+        umtlib.set_materials(pr.sigt, pr.sigs, pr.tau)
+        umtlib.set_psi(pr.psi0, None)
+        st = np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi)
+        single.append(umtlib.sweep(st, precision=capi.UMT_FP32))
+    ids = []
+    for pr in probs:
+        cid = umtlib.context_create()
+        umtlib.context_select(cid)
+        umtlib.init(pr.mesh, pr.omega, pr.weight, pr.ngr, flags=2 | 8)
+        umtlib.set_materials(pr.sigt, pr.sigs, pr.tau)
+        umtlib.set_psi(pr.psi0, None)
+        umtlib.set_source(np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi))
+        ids.append(cid)
+    umtlib.context_select(0)
+    ms = umtlib.batch_sweep(ids, capi.UMT_FP32)
+    assert ms > 0
+    for cid, pr, ref in zip(ids, probs, single):
+        umtlib.context_select(cid)
+        phi = umtlib.get_phi(pr.mesh.ncornr, pr.ngr)
+        assert np.array_equal(phi, ref)
+    umtlib.context_select(0)
+    for cid in ids:
+        umtlib.context_destroy(cid)

@@ -39,7 +39,7 @@ class UmtQuad(C.Structure):
 
 class UmtSIParams(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_iters", C.c_int), ("rel_tol", C.c_double),
-                ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int)]
+                ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int), ("warm_start", C.c_int)]
 
 
 class UmtSIResult(C.Structure):
@@ -77,7 +77,10 @@ def load():
                   "umt103_get_phi", "umt103_source_iterate", "umt103_tally",
                   "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry",
                   "umt103_last_timing", "umt103_launches_per_sweep", "umt103_select_device",
-                  "umt103_set_group_tile", "umt103_tally_precision", "umt103_set_sweep_mode"):
+                  "umt103_set_group_tile", "umt103_tally_precision", "umt103_set_sweep_mode",
+                  "umt103_set_gta", "umt103_context_create",
+                  "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
+                  "umt103_batch_sweep"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
@@ -91,7 +94,9 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_get_schedule", "umt103_get_geometry", "umt103_last_sweep_ms",
             "umt103_error_string", "umt103_last_timing", "umt103_launches_per_sweep",
             "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision",
-            "umt103_set_sweep_mode"]
+            "umt103_set_sweep_mode", "umt103_set_gta",
+            "umt103_context_create", "umt103_context_select", "umt103_context_current",
+            "umt103_context_destroy", "umt103_batch_sweep"]
 
 
 def check(rc):
@@ -183,8 +188,8 @@ class Library:
     def sweep_resident(self, savePsi=False, precision=UMT_FP64):
         check(self.lib.umt103_sweep_resident(int(bool(savePsi)), int(precision)))
 
-    def get_phi(self):
-        Phi = np.zeros((self.nc, self.G))
+    def get_phi(self, nc=None, G=None):
+        Phi = np.zeros((nc or self.nc, G or self.G))
         check(self.lib.umt103_get_phi(_d(Phi)))
         return Phi
 
@@ -200,10 +205,10 @@ class Library:
         return n
 
     def source_iterate(self, precision=UMT_FP64, max_iters=50, rel_tol=1e-8, q_ext=None, save_psi=True,
-                       use_gta=False, allow_notconv=False):
+                       use_gta=False, allow_notconv=False, warm_start=False):
         q = _c(q_ext, np.float64)
         prm = UmtSIParams(int(precision), int(max_iters), float(rel_tol), int(bool(use_gta)), _d(q),
-                          int(bool(save_psi)))
+                          int(bool(save_psi)), int(bool(warm_start)))
         res = UmtSIResult()
         rc = self.lib.umt103_source_iterate(C.byref(prm), C.byref(res))
         if rc != 0 and not (allow_notconv and rc == -8):
@@ -221,8 +226,29 @@ class Library:
         return dict(EnergyRadiation=t.EnergyRadiation, PowerEscape=t.PowerEscape,
                     PowerIncident=t.PowerIncident, PowerAbsorbed=t.PowerAbsorbed)
 
+    def context_create(self):
+        cid = C.c_int(0)
+        check(self.lib.umt103_context_create(C.byref(cid)))
+        return cid.value
+
+    def context_select(self, cid):
+        check(self.lib.umt103_context_select(int(cid)))
+
+    def context_destroy(self, cid):
+        check(self.lib.umt103_context_destroy(int(cid)))
+
+    def batch_sweep(self, ids, precision=UMT_FP32):
+        arr = (C.c_int * len(ids))(*ids)
+        ms = C.c_double(0.0)
+        check(self.lib.umt103_batch_sweep(arr, len(ids), int(precision), C.byref(ms)))
+        return ms.value
+
     def set_group_tile(self, lanes_per_zone, groups_per_lane):
         check(self.lib.umt103_set_group_tile(int(lanes_per_zone), int(groups_per_lane)))
+
+    def set_gta(self, max_krylov=10, tol=1e-4, spectrum=0):
+        self.lib.umt103_set_gta.argtypes = [C.c_int, C.c_double, C.c_int]
+        check(self.lib.umt103_set_gta(int(max_krylov), float(tol), int(spectrum)))
 
     def set_sweep_mode(self, mode):
         check(self.lib.umt103_set_sweep_mode(int(mode)))

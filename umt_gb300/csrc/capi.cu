@@ -8,7 +8,12 @@
 
 namespace umt {
 
-Ctx g;
+// Contexts: slot 0 always exists; umt103_context_create adds more (independent
+// problems resident together, e.g. for a batched launch).  Every entry point
+// works on the current context.
+static Ctx g_default;
+Ctx *g_cur = &g_default;
+static std::vector<Ctx *> g_ctx{&g_default};
 std::string g_err;
 
 int set_error(int code, const char *fmt, ...) {
@@ -42,12 +47,12 @@ static void dfree(T *&p) {
 static void free_ctx(Ctx &c);
 
 static void free_all() {
-  if (g.gta) {
-    free_ctx(*g.gta);
-    delete g.gta;
-    g.gta = nullptr;
+  if (cur().gta) {
+    free_ctx(*cur().gta);
+    delete cur().gta;
+    cur().gta = nullptr;
   }
-  free_ctx(g);
+  free_ctx(cur());
 }
 
 static void free_ctx(Ctx &c) {
@@ -98,11 +103,97 @@ const char *umt103_error_string(void) { return g_err.c_str(); }
 
 void umt103_finalize(void) { free_all(); }
 
+int umt103_context_create(int *id) {
+  if (!id) return set_error(UMT_ERR_ARG, "null id");
+  for (size_t k = 1; k < g_ctx.size(); ++k)
+    if (!g_ctx[k]) { g_ctx[k] = new Ctx(); *id = (int)k; return 0; }
+  g_ctx.push_back(new Ctx());
+  *id = (int)g_ctx.size() - 1;
+  return 0;
+}
+
+int umt103_context_select(int id) {
+  if (id < 0 || id >= (int)g_ctx.size() || !g_ctx[id]) return set_error(UMT_ERR_ARG, "no context %d", id);
+  g_cur = g_ctx[id];
+  return 0;
+}
+
+int umt103_context_current(void) {
+  for (size_t k = 0; k < g_ctx.size(); ++k)
+    if (g_ctx[k] == g_cur) return (int)k;
+  return -1;
+}
+
+int umt103_context_destroy(int id) {
+  if (id <= 0 || id >= (int)g_ctx.size() || !g_ctx[id]) return set_error(UMT_ERR_ARG, "cannot destroy context %d", id);
+  Ctx *victim = g_ctx[id], *keep = g_cur;
+  g_cur = victim;
+  free_all();
+  delete victim;
+  g_ctx[id] = nullptr;
+  g_cur = (keep == victim) ? &g_default : keep;
+  return 0;
+}
+
+// One CUDA graph that sweeps several contexts at once: each context's captured
+// sweep graph (source conversion, every dependency stage, tally) becomes an
+// independent child node, so problems of different sizes, group counts and
+// direction counts run concurrently from a single launch.
+int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
+  if (!ids || n <= 0) return set_error(UMT_ERR_ARG, "empty batch");
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
+  Ctx *keep = g_cur;
+  std::vector<cudaGraph_t> children;
+  int rc = 0;
+  for (int k = 0; k < n && !rc; ++k) {
+    const int id = ids[k];
+    if (id < 0 || id >= (int)g_ctx.size() || !g_ctx[id] || !g_ctx[id]->ready) {
+      rc = set_error(UMT_ERR_ARG, "batch: context %d not initialised", id);
+      break;
+    }
+    g_cur = g_ctx[id];
+    cudaGraph_t gr = nullptr;
+    rc = capture_sweep_graph(*g_cur, precision, &gr);
+    if (!rc) children.push_back(gr);
+  }
+  g_cur = keep;
+  cudaGraph_t parent = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t st = g_ctx[ids[0]] ? g_ctx[ids[0]]->stream : nullptr;
+  if (!rc) {
+    cudaError_t e = cudaGraphCreate(&parent, 0);
+    for (size_t k = 0; k < children.size() && e == cudaSuccess; ++k) {
+      cudaGraphNode_t node;
+      e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, children[k]);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, parent, 0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && ms) {
+      float f = 0.f;
+      e = cudaEventElapsedTime(&f, e0, e1);
+      *ms = f;
+    }
+    if (e != cudaSuccess) rc = set_error(UMT_ERR_CUDA, "batch sweep: %s", cudaGetErrorString(e));
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (parent) cudaGraphDestroy(parent);
+  for (auto gr : children) cudaGraphDestroy(gr);
+  return rc;
+}
+
 static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags);
 
 int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
   free_all();
-  int rc = init_ctx(g, m, q, ngr, flags);
+  int rc = init_ctx(cur(), m, q, ngr, flags);
   if (rc) return rc;
   // The grey (GTA) problem: same mesh, level-symmetric S2 (8 directions,
   // |mu| = |eta| = |xi| = 1/sqrt(3), equal weights summing to 4 pi), one group,
@@ -117,8 +208,8 @@ int umt103_init(const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
       wt[a] = w;
     }
     UmtQuad q2{8, om, wt};
-    g.gta = new Ctx();
-    rc = init_ctx(*g.gta, m, &q2, 1, 1);
+    cur().gta = new Ctx();
+    rc = init_ctx(*cur().gta, m, &q2, 1, 1);
     if (rc) {
       free_all();
       return rc;
@@ -289,7 +380,7 @@ static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int fla
 }
 
 int umt103_set_materials(const double *sigt, const double *sigs, double tau) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (!sigt) return set_error(UMT_ERR_ARG, "sigt is required");
   const size_t nzG = (size_t)c.nz * c.G;
@@ -313,7 +404,7 @@ __global__ void k_f2d(size_t n, const float *x, double *y) {
 }
 
 int umt103_set_psi(const double *Psi, const double *PsiB) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   const size_t psiN = (size_t)c.A * c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   double *tmp = nullptr;
@@ -333,7 +424,7 @@ int umt103_set_psi(const double *Psi, const double *PsiB) {
 }
 
 int umt103_get_psi(double *Psi, double *PsiB, int precision) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   const size_t psiN = (size_t)c.A * c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   if (precision == UMT_FP64) {
@@ -354,7 +445,7 @@ int umt103_get_psi(double *Psi, double *PsiB, int precision) {
 }
 
 int umt103_set_source(const double *STotal) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   const size_t ncG = (size_t)c.nc * c.G;
   if (STotal) UMT_CUDA(cudaMemcpy(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice));
@@ -363,7 +454,7 @@ int umt103_set_source(const double *STotal) {
 }
 
 static int sweep_core(int savePsi, int precision) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
@@ -388,19 +479,19 @@ static int sweep_core(int savePsi, int precision) {
 }
 
 int umt103_sweep_resident(int savePsi, int precision) {
-  if (!g.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!cur().ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   return sweep_core(savePsi, precision);
 }
 
 int umt103_get_phi(double *PhiTotal) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   UMT_CUDA(cudaMemcpy(PhiTotal, c.Phi, (size_t)c.nc * c.G * 8, cudaMemcpyDeviceToHost));
   return 0;
 }
 
 int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double *PsiB_inout, int precision) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
@@ -434,30 +525,39 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   return 0;
 }
 
-double umt103_last_sweep_ms(void) { return g.lastMs; }
+double umt103_last_sweep_ms(void) { return cur().lastMs; }
 
 int umt103_last_timing(double *out3) {
   if (!out3) return set_error(UMT_ERR_ARG, "null output");
-  out3[0] = g.lastMs; out3[1] = g.lastKernMs; out3[2] = g.lastTallyMs;
+  out3[0] = cur().lastMs; out3[1] = cur().lastKernMs; out3[2] = cur().lastTallyMs;
   return 0;
 }
 
 int umt103_launches_per_sweep(int precision) {
   if (precision != 0 && precision != 1) return set_error(UMT_ERR_ARG, "precision");
-  return g.launchesPerSweep[precision];
+  return cur().launchesPerSweep[precision];
+}
+
+int umt103_set_gta(int max_krylov, double tol, int spectrum) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (max_krylov < 1 || !(tol > 0.0) || spectrum < 0 || spectrum > 1)
+    return set_error(UMT_ERR_ARG, "bad GTA options");
+  c.gtaMaxKrylov = max_krylov; c.gtaTol = tol; c.gtaSpectrum = spectrum;
+  return 0;
 }
 
 int umt103_set_sweep_mode(int mode) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
-  if (mode != 0 && mode != 1) return set_error(UMT_ERR_ARG, "sweep mode must be 0 or 1");
+  if (mode < 0 || mode > 2) return set_error(UMT_ERR_ARG, "sweep mode must be 0, 1 or 2");
   if (c.sweepMode != mode) invalidate_graphs(c);
   c.sweepMode = mode;
   return 0;
 }
 
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   invalidate_graphs(c);
   if (lanes_per_zone == 0 && groups_per_lane == 0) { c.tileGT = 0; c.tileGPL = 0; return 0; }
@@ -476,7 +576,7 @@ int umt103_select_device(int device) {
 }
 
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (angle < 0 || angle >= c.A) return set_error(UMT_ERR_ARG, "angle out of range");
   int h = 0;
@@ -487,7 +587,7 @@ int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles) {
 }
 
 int umt103_get_schedule(int *level, int *nHyperPlanes) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (level) UMT_CUDA(cudaMemcpy(level, c.sch.level, (size_t)c.A * c.nz * sizeof(int), cudaMemcpyDeviceToHost));
   if (nHyperPlanes) UMT_CUDA(cudaMemcpy(nHyperPlanes, c.sch.nHyper, c.A * sizeof(int), cudaMemcpyDeviceToHost));
@@ -495,7 +595,7 @@ int umt103_get_schedule(int *level, int *nHyperPlanes) {
 }
 
 int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   const size_t nA = (size_t)c.nc * UMT_MAXCF * 3;
   if (A_fp) UMT_CUDA(cudaMemcpy(A_fp, c.A_fp, nA * 8, cudaMemcpyDeviceToHost));
@@ -560,7 +660,7 @@ static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps) {
 }
 
 int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (!prm || !res) return set_error(UMT_ERR_ARG, "null params/result");
   const int prec = prm->precision;
@@ -585,6 +685,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
     q = c.qExt;
   }
   const int maxit = prm->max_iters > 0 ? prm->max_iters : 50;
+  if (!prm->warm_start) UMT_CUDA(cudaMemsetAsync(c.Phi, 0, ncG * 8, c.stream));
   UMT_CUDA(cudaMemcpyAsync(c.PhiPrev, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
   cudaEvent_t t0, t1;
   UMT_CUDA(cudaEventCreate(&t0)); UMT_CUDA(cudaEventCreate(&t1));
@@ -597,7 +698,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
     TRY(launch_build_source(c, q));
     TRY(launch_sweep_once(c, prec, true));
     ++sweeps;
-    if (prm->use_gta) TRY(gta_solve(c, 10, 1.0e-4, &greySweeps));
+    if (prm->use_gta) TRY(gta_solve(c, c.gtaMaxKrylov, c.gtaTol, &greySweeps));
     TRY(launch_change_norm(c, c.PhiPrev, c.red));
     double h[2];
     UMT_CUDA(cudaMemcpyAsync(h, c.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -622,12 +723,12 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
 }
 
 int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *t) {
-  if (!g.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
-  return umt103_tally_precision(siga, speed_light, g.psi64[0] ? UMT_FP64 : UMT_FP32, t);
+  if (!cur().ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  return umt103_tally_precision(siga, speed_light, cur().psi64[0] ? UMT_FP64 : UMT_FP32, t);
 }
 
 int umt103_tally_precision(const double *siga, double speed_light, int precision, UmtEnergyTally *t) {
-  Ctx &c = g;
+  Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");

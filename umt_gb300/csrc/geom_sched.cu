@@ -170,8 +170,18 @@ __global__ void k_projections(int A, int nc, const double *omega, const int *nCF
     double vf = 0.0, ve = 0.0;
     if (cf < nCFaces[c]) {
       const double *o = omega + 3 * a;
-      vf = dot3(o, A_fp + ((size_t)c * UMT_MAXCF + cf) * 3);
-      ve = dot3(o, A_ez + ((size_t)c * UMT_MAXCF + cf) * 3);
+      const double *af = A_fp + ((size_t)c * UMT_MAXCF + cf) * 3;
+      const double *ae = A_ez + ((size_t)c * UMT_MAXCF + cf) * 3;
+      vf = dot3(o, af);
+      ve = dot3(o, ae);
+      // A face parallel to the direction (Omega.A = 0 in exact arithmetic, e.g.
+      // a 45-degree face and an S2 direction) would otherwise get a rounding-
+      // noise sign per corner face; such projections are set to exactly zero,
+      // so the face carries no flux and creates no dependency.
+      const double nf = fabs(af[0]) + fabs(af[1]) + fabs(af[2]);
+      const double ne = fabs(ae[0]) + fabs(ae[1]) + fabs(ae[2]);
+      if (fabs(vf) <= 1.0e-12 * nf) vf = 0.0;
+      if (fabs(ve) <= 1.0e-12 * ne) ve = 0.0;
     }
     if (afp64) { afp64[i] = vf; aez64[i] = ve; }
     if (afp32) { afp32[i] = (float)vf; aez32[i] = (float)ve; }

@@ -110,7 +110,7 @@ __global__ void k_energy(int nc, int nb, int A, int G, const int *cToZone, const
 // per zone as the shape of the current residual, |sigma_s,g dphi_g| summed
 // over the zone's corners and normalised.
 // ---------------------------------------------------------------------------
-__global__ void k_gta_spectrum(int nz, int G, double tau, const int *numCorner, const int *cOffSet,
+__global__ void k_gta_spectrum(int nz, int G, double tau, int mode, const int *numCorner, const int *cOffSet,
                                const double *Volume, const double *Sigt, const double *SigS, const double *Phi,
                                const double *Prev, double *chi, double *greySigt, double *greySigs) {
   for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
@@ -122,6 +122,9 @@ __global__ void k_gta_spectrum(int nz, int G, double tau, const int *numCorner, 
         const size_t e = (size_t)(c0 + k) * G + g;
         r += Volume[c0 + k] * fabs(SigS[(size_t)z * G + g] * (Phi[e] - Prev[e]));
       }
+      // mode 1: weight by the infinite-medium amplification 1/(1-c) of the
+      // group's residual, which favours the slowly converging groups
+      if (mode == 1) r /= fmax(1.0 - SigS[(size_t)z * G + g] / Sigt[(size_t)z * G + g], 1.0e-6);
       chi[(size_t)z * G + g] = r;
       rsum += r;
     }
@@ -206,7 +209,7 @@ __global__ void k_gta_correct(int nc, int G, const int *cToZone, const double *c
 int gta_prepare(Ctx &c) {
   Ctx &q = *c.gta;
   const int B = 152 * 4;
-  k_gta_spectrum<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, c.G, c.tau, c.numCorner, c.cOffSet, c.Volume,
+  k_gta_spectrum<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, c.G, c.tau, c.gtaSpectrum, c.numCorner, c.cOffSet, c.Volume,
                                                           c.Sigt, c.SigS, c.Phi, c.PhiPrev, c.gtaChi, q.Sigt,
                                                           c.gtaSigS);
   UMT_CUDA(cudaMemcpyAsync(q.SigS, c.gtaSigS, c.nz * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));

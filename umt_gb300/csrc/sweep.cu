@@ -377,17 +377,37 @@ static int sweep_via_graph(Ctx &c, int precision) {
   return 0;
 }
 
+static int prepare_precision(Ctx &c, int precision) {
+  // one-time preparation; must not run inside a capture
+  if (precision == 1) {
+    if (c.tileGT == 0) default_tile(c.G, &c.tileGT, &c.tileGPL);
+    if (!c.rec32Ready && c.tileGT > 0) {
+      int rc = prepare_sweep32(c);
+      if (rc) return rc;
+      c.rec32Ready = true;
+    }
+  }
+  return 0;
+}
+
+// A fresh, uninstantiated graph of one sweep of this context (the caller owns
+// it); used to combine several contexts into one launch.
+int capture_sweep_graph(Ctx &c, int precision, cudaGraph_t *out) {
+  TRY_RC(prepare_precision(c, precision));
+  const int cur = precision == 0 ? c.cur64 : c.cur32;
+  UMT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  int rc = precision == 0 ? enqueue_sweep<double>(c, cur) : enqueue_sweep<float>(c, cur);
+  cudaGraph_t gr = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c.stream, &gr);
+  if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+  if (e != cudaSuccess) return set_error(-3, "graph capture: %s", cudaGetErrorString(e));
+  *out = gr;
+  return 0;
+}
+
 int launch_sweep_once(Ctx &c, int precision, bool /*tally*/) {
   if (c.useGraphs) {
-    // one-time preparation must not be captured
-    if (precision == 1) {
-      if (c.tileGT == 0) default_tile(c.G, &c.tileGT, &c.tileGPL);
-      if (!c.rec32Ready && c.tileGT > 0) {
-        int rc = prepare_sweep32(c);
-        if (rc) return rc;
-        c.rec32Ready = true;
-      }
-    }
+    TRY_RC(prepare_precision(c, precision));
     return sweep_via_graph(c, precision);
   }
   if (precision == 0) return enqueue_sweep<double>(c, c.cur64);

@@ -66,6 +66,7 @@ struct Ctx {
   bool rec32Ready = false;
   int tileGT = 0, tileGPL = 0;                  // FP32 group tile (0: choose)
   int sweepMode = 0;                            // FP32: 0 = one launch per stage, 1 = persistent
+  bool useCompact = true;                       // FP32: compact-list kernel where the tile allows
   int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
   int *ticket = nullptr;                        // persistent-mode work ticket
   Schedule sch;
@@ -100,9 +101,13 @@ struct Ctx {
   double *gtaChi = nullptr;                     // [nz][G] correction spectrum
   double *gtaVec = nullptr;                     // [8][nc] BiCGStab vectors
   double *gtaSigS = nullptr;                    // [nz] grey scattering (for inner products)
+  int gtaMaxKrylov = 10;                        // BiCGStab iterations per correction (2 grey sweeps each)
+  double gtaTol = 1.0e-4;                       // BiCGStab relative residual
+  int gtaSpectrum = 0;                          // correction spectrum (see k_gta_spectrum)
 };
 
-extern Ctx g;
+extern Ctx *g_cur;
+inline Ctx &cur() { return *g_cur; }
 extern std::string g_err;
 
 int set_error(int code, const char *fmt, ...);
@@ -120,7 +125,7 @@ int launch_geometry(Ctx &c);
 int launch_projections(Ctx &c);
 int build_schedule(Ctx &c);
 // launchers (sweep TU)
-int capture_sweep_graph(Ctx &c, int precision);
+int capture_sweep_graph(Ctx &c, int precision, cudaGraph_t *out);
 int launch_sweep_once(Ctx &c, int precision, bool tally);
 int launch_tally(Ctx &c, int precision);
 void invalidate_graphs(Ctx &c);
