@@ -189,6 +189,32 @@ int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *tally);
 int umt103_tally_precision(const double *siga, double speed_light, int precision,
                            UmtEnergyTally *tally);
 
+/*
+ * umt103_tally_noalloc: the energy edits of umt103_tally_precision for
+ * callers that cannot let a library allocate device memory during a call --
+ * host codes whose memory pool must account for every device byte, or runs
+ * that have already reserved all free device memory, where an allocation
+ * inside the library would fail or escape the pool.  No counterpart in the
+ * reference (its edits run on the host, aux/rtedit.F90).
+ *
+ *   siga_dev    absorption opacity Siga(G,nzones) already in device memory,
+ *               or NULL (PowerAbsorbed is then 0); nothing is copied;
+ *   precision   UMT_FP64 or UMT_FP32 angular flux.
+ *
+ * It allocates nothing: the reduction works in a fixed scratch array that is
+ * part of the loaded library (one copy on every GPU that loads it, held until
+ * the process exits), and the result is summed in a fixed order, so repeated
+ * calls give bit-identical results.  The scratch need not start at zero:
+ * each call writes every value it later reads.  Limit: max(ncornr*G, nangles*nbelem)
+ * must not exceed UMT_NOALLOC_MAX_BLOCKS*4096 elements (UMT_ERR_ARG with a
+ * message otherwise).  The first call on a device looks up the scratch
+ * address on that device; make that first call before any stream capture.
+ * All calls share the scratch: calls that overlap on the GPU (other threads,
+ * other streams of the same device) race and must be serialised by the caller.
+ */
+#define UMT_NOALLOC_MAX_BLOCKS 32768
+int umt103_tally_noalloc(const double *siga_dev, double speed_light, int precision,
+                         UmtEnergyTally *tally);
 
 /* Schedule statistics for one direction. */
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);

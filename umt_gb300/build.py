@@ -25,6 +25,7 @@ UNITS = {
     "sweep.cu": [],
     "sweep32.cu": [],
     "si.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -78,13 +78,14 @@ def load():
                   "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry",
                   "umt103_last_timing", "umt103_launches_per_sweep", "umt103_select_device",
                   "umt103_set_group_tile", "umt103_tally_precision", "umt103_set_sweep_mode",
-                  "umt103_set_gta", "umt103_context_create",
+                  "umt103_set_gta", "umt103_tally_noalloc", "umt103_context_create",
                   "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
                   "umt103_batch_sweep"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
         _lib.umt103_tally_precision.argtypes = [_dp, C.c_double, C.c_int, C.POINTER(UmtEnergyTally)]
+        _lib.umt103_tally_noalloc.argtypes = [C.c_void_p, C.c_double, C.c_int, C.POINTER(UmtEnergyTally)]
     return _lib
 
 
@@ -94,7 +95,7 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_get_schedule", "umt103_get_geometry", "umt103_last_sweep_ms",
             "umt103_error_string", "umt103_last_timing", "umt103_launches_per_sweep",
             "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision",
-            "umt103_set_sweep_mode", "umt103_set_gta",
+            "umt103_set_sweep_mode", "umt103_set_gta", "umt103_tally_noalloc",
             "umt103_context_create", "umt103_context_select", "umt103_context_current",
             "umt103_context_destroy", "umt103_batch_sweep"]
 
@@ -223,6 +224,15 @@ class Library:
             check(self.lib.umt103_tally(_d(siga), C.c_double(speed_light), C.byref(t)))
         else:
             check(self.lib.umt103_tally_precision(_d(siga), C.c_double(speed_light), int(precision), C.byref(t)))
+        return dict(EnergyRadiation=t.EnergyRadiation, PowerEscape=t.PowerEscape,
+                    PowerIncident=t.PowerIncident, PowerAbsorbed=t.PowerAbsorbed)
+
+    def tally_noalloc(self, siga_dev_ptr=None, speed_light=299.792458, precision=UMT_FP64):
+        """Energy edits without device allocation; siga_dev_ptr is a device
+        address (int) of Siga(G,nzones) in FP64, or None."""
+        t = UmtEnergyTally()
+        check(self.lib.umt103_tally_noalloc(C.c_void_p(siga_dev_ptr) if siga_dev_ptr else None,
+                                            C.c_double(speed_light), int(precision), C.byref(t)))
         return dict(EnergyRadiation=t.EnergyRadiation, PowerEscape=t.PowerEscape,
                     PowerIncident=t.PowerIncident, PowerAbsorbed=t.PowerAbsorbed)
 
