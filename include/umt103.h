@@ -242,13 +242,17 @@ int umt103_last_timing(double *out3);
  * (gpu/GPU_SweepUCBxyz.cu:30-31). */
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane);
 
-/* FP32 sweep scheduling: 0 (default) = one kernel launch per dependency stage
- * (the hyperplane loop of snac/SweepUCBxyz.F90:103, all directions at once),
- * with the compact face-list kernel where the group tile allows it;
- * 2 = one kernel launch per stage, unrolled corner-slot kernel;
- * 1 = one persistent launch in which each (direction, zone) pair
- * starts as soon as its upwind zones have finished (bounded waits; a wait that
- * gives up makes the sweep return UMT_ERR_TIMEOUT). */
+/* FP32 sweep kernel and scheduling.  Modes 0, 2 and 3 launch one kernel per
+ * dependency stage (the hyperplane loop of snac/SweepUCBxyz.F90:103, all
+ * directions at once):
+ *   0 (default) zone-program kernel: each (direction, zone) pair runs a
+ *     compact list of its face operations built once on the device (group
+ *     tiles with 2 or 4 groups per lane; other tiles fall back to mode 2);
+ *   2 unrolled corner-slot kernel;
+ *   3 compact face-list kernel (corner-face slots classified per sweep);
+ *   1 one persistent launch in which each (direction, zone) pair starts as
+ *     soon as its upwind zones have finished (bounded waits; a wait that
+ *     gives up makes the sweep return UMT_ERR_TIMEOUT). */
 int umt103_set_sweep_mode(int mode);
 
 /* Number of kernels one sweep of the given precision launches (>= 0). */

@@ -79,10 +79,13 @@ def test_fp32_sweep_tolerance(umtlib):
     assert rel_err(Psi, ref["Psi"]) < 1e-4
 
 
+@pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("G,tile", [(16, (16, 1)), (16, (8, 2)), (16, (4, 4)), (2, (1, 2)),
-                                    (2, (2, 1)), (8, (2, 4)), (32, (8, 4))])
-def test_fp32_group_tiles(umtlib, G, tile):
-    """Every group tile of the production FP32 kernel agrees with the oracle."""
+                                    (2, (2, 1)), (8, (2, 4)), (32, (8, 4)), (64, (32, 2)),
+                                    (4, (2, 2)), (32, (16, 2))])
+def test_fp32_group_tiles(umtlib, G, tile, mode):
+    """Every group tile of the FP32 zone-program kernel (mode 0) and of the
+    corner-slot kernel (mode 2) agrees with the oracle."""
     prob = synthetic_problem((2, 2, 1), 2, 2, G, seed=4, time_dependent=True)
     m = prob.mesh
     STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
@@ -91,6 +94,7 @@ def test_fp32_group_tiles(umtlib, G, tile):
     umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
     umtlib.set_psi(prob.psi0, None)
     umtlib.set_group_tile(*tile)
+    umtlib.set_sweep_mode(mode)
     PsiB = np.zeros((len(prob.weight), m.nbelem, G))
     Phi = umtlib.sweep(STotal, savePsi=True, PsiB=PsiB, precision=capi.UMT_FP32)
     Psi, _ = umtlib.get_psi(capi.UMT_FP32)
@@ -99,9 +103,11 @@ def test_fp32_group_tiles(umtlib, G, tile):
     assert rel_err(PsiB, ref["PsiB"]) < 1e-4
 
 
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_fp32_sweep_modes(umtlib, mode):
-    """Per-stage launches (0) and the persistent dependency-driven launch (1)."""
+    """Per-stage launches of the zone-program (0), corner-slot (2) and
+    compact face-list (3) kernels, and the persistent dependency-driven
+    launch (1)."""
     prob = synthetic_problem((3, 2, 2), 4, 4, 16, seed=6, time_dependent=True)
     m = prob.mesh
     STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)

@@ -24,6 +24,7 @@ UNITS = {
     "geom_sched.cu": ["-fmad=false"],
     "sweep.cu": [],
     "sweep32.cu": [],
+    "sweep32p.cu": [],
     "si.cu": [],
     "noalloc.cu": [],
 }

@@ -64,7 +64,7 @@ static void free_ctx(Ctx &c) {
   dfree(c.px); dfree(c.A_fp); dfree(c.A_ez); dfree(c.Volume); dfree(c.VolumeZone); dfree(c.A_bdy);
   dfree(c.Afp_raw); dfree(c.omega); dfree(c.weight); dfree(c.weight32);
   dfree(c.afp64); dfree(c.aez64); dfree(c.afp32); dfree(c.aez32);
-  dfree(c.rec32); dfree(c.conn32); dfree(c.vol32);
+  dfree(c.rec32); dfree(c.conn32); dfree(c.vol32); dfree(c.prog32); dfree(c.hdr32);
   Schedule &s = c.sch;
   dfree(s.items); dfree(s.items2); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
   dfree(s.needInit); dfree(c.dep); dfree(c.ticket);
@@ -550,7 +550,7 @@ int umt103_set_gta(int max_krylov, double tol, int spectrum) {
 int umt103_set_sweep_mode(int mode) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
-  if (mode < 0 || mode > 2) return set_error(UMT_ERR_ARG, "sweep mode must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) return set_error(UMT_ERR_ARG, "sweep mode must be 0, 1, 2 or 3");
   if (c.sweepMode != mode) invalidate_graphs(c);
   c.sweepMode = mode;
   return 0;

@@ -22,6 +22,7 @@
 // touches only its own groups there; the staged corner records are shared by
 // the team and published with one __syncwarp over the team's lanes.
 #include "umt_common.cuh"
+#include "sweep32_util.cuh"
 
 namespace umt {
 
@@ -271,10 +272,6 @@ __device__ __forceinline__ void sweep_zone(const Sweep32P &p, const uint2 w, con
   }
 }
 
-__device__ __forceinline__ unsigned team_mask(int GT, int tid) {
-  return (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
-}
-
 // ---------------------------------------------------------------------------
 // Compact-list kernel (groups_per_lane = 2 or 4).  After the zone's corner
 // records are staged, the team classifies its 24 corner-face slots with warp
@@ -286,39 +283,6 @@ __device__ __forceinline__ unsigned team_mask(int GT, int tid) {
 // as cp.async copies into shared memory.  Arithmetic on group pairs uses
 // Blackwell's paired FP32 instructions (FFMA2/FMUL2/FADD2).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async(void *smem, const void *gmem, int bytes) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  if (bytes == 16)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-  else if (bytes == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\n" ::);
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
-
-__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
-
-template <int NP>
-__device__ __forceinline__ void ld2(const float *p, float2 (&v)[NP]) {
-  if constexpr (NP == 2) {
-    const float4 t = *reinterpret_cast<const float4 *>(p);
-    v[0] = make_float2(t.x, t.y); v[1] = make_float2(t.z, t.w);
-  } else {
-    v[0] = *reinterpret_cast<const float2 *>(p);
-  }
-}
-template <int NP>
-__device__ __forceinline__ void st2(float *p, const float2 (&v)[NP]) {
-  if constexpr (NP == 2)
-    *reinterpret_cast<float4 *>(p) = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
-  else
-    *reinterpret_cast<float2 *>(p) = v[0];
-}
-
 template <int GT, int GPL>
 __global__ void __launch_bounds__(SW32_NT) k_sweep32v4(Sweep32P p, int stage) {
   static_assert(GPL == 2 || GPL == 4, "paired kernel");
@@ -651,7 +615,7 @@ __global__ void k_conn(int nc, const int *nCFaces, const int *cFP, const int *cE
 }
 
 // Let a kernel use all the shared memory its static arrays leave free.
-static int allow_dynamic_smem(const void *fn) {
+int allow_dynamic_smem(const void *fn) {
   int dev = 0, optin = 0;
   UMT_CUDA(cudaGetDevice(&dev));
   UMT_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -688,7 +652,7 @@ int prepare_sweep32(Ctx &c) {
   k_conn<<<(c.nc + 255) / 256, 256, 0, c.stream>>>(c.nc, c.nCFaces, c.cFP, c.cEZ, (int4 *)c.conn32, c.vol32,
                                                    c.Volume);
   UMT_CUDA(cudaGetLastError());
-  return 0;
+  return prepare_prog32(c);
 }
 
 // Group tile: GT lanes per (direction, zone), GPL groups per lane, G = GT*GPL.
@@ -731,8 +695,12 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   UMT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const int stride4 = 40 * c.G + ((((c.G - (40 * c.G) % 32) % 32) + 32) % 32);
   const size_t smem4 = (size_t)TEAMS * stride4 * sizeof(float);
+  if (c.sweepMode == 0) {
+    const int rc = enqueue_sweep32p(c, cur, GT, GPL);
+    if (rc <= 0) return rc;                        // 1: no program kernel for this tile
+  }
 #define UMT_LAUNCH4(gt, gpl)                                                                       \
-  if (GT == gt && GPL == gpl && c.sweepMode == 0) {                                                \
+  if (GT == gt && GPL == gpl && c.sweepMode == 3) {                                                \
     Sweep32P p4 = p;                                                                               \
     p4.stride = stride4;                                                                           \
     for (int s = 0; s < c.sch.nStages; ++s) {                                                      \
@@ -742,7 +710,7 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
     UMT_CUDA(cudaGetLastError());                                                                  \
     return 0;                                                                                      \
   }
-  if (c.sweepMode == 0) {
+  if (c.sweepMode == 3) {
     UMT_LAUNCH4(1, 2) UMT_LAUNCH4(1, 4) UMT_LAUNCH4(2, 2) UMT_LAUNCH4(2, 4) UMT_LAUNCH4(4, 2) UMT_LAUNCH4(4, 4)
     UMT_LAUNCH4(8, 2) UMT_LAUNCH4(8, 4) UMT_LAUNCH4(16, 2) UMT_LAUNCH4(16, 4) UMT_LAUNCH4(32, 2) UMT_LAUNCH4(32, 4)
   }

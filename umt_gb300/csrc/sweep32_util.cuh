@@ -1,0 +1,57 @@
+// sweep32_util.cuh -- device helpers shared by the FP32 sweep kernels
+// (sweep32.cu, sweep32p.cu): team lane masks, asynchronous global->shared
+// copies, and group-pair (float2) loads and stores for the paired FP32
+// instructions (FFMA2/FMUL2/FADD2) of sm_100-class GPUs.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace umt {
+
+// Lanes of the calling thread's team (GT consecutive lanes of one warp).
+__device__ __forceinline__ unsigned team_mask(int GT, int tid) {
+  return (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
+}
+
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem, int bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if (bytes == 16)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+  else if (bytes == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+}
+// 16-byte copy that bypasses L1 (streamed data read once per block).
+__device__ __forceinline__ void cp_async16_cg(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+template <int NP>
+__device__ __forceinline__ void ld2(const float *p, float2 (&v)[NP]) {
+  if constexpr (NP == 2) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = make_float2(t.x, t.y); v[1] = make_float2(t.z, t.w);
+  } else {
+    v[0] = *reinterpret_cast<const float2 *>(p);
+  }
+}
+template <int NP>
+__device__ __forceinline__ void st2(float *p, const float2 (&v)[NP]) {
+  if constexpr (NP == 2)
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+  else
+    *reinterpret_cast<float2 *>(p) = v[0];
+}
+
+// Let a kernel use all the shared memory its static arrays leave free
+// (sweep32.cu).
+int allow_dynamic_smem(const void *fn);
+
+}  // namespace umt

@@ -1,0 +1,595 @@
+// sweep32p.cu -- FP32 UCB sweep driven by precompiled zone programs.
+//
+// The arithmetic is that of snac/SweepUCBxyz.F90:103-312 (and of the kernels
+// in sweep32.cu); what changes is how a (direction, zone) pair finds its work.
+// The corner-face geometry of a zone, seen from one direction, does not change
+// between sweeps, so the classification the sweep would otherwise redo every
+// time -- which FP faces are incoming, which EZ faces carry flux and which of
+// those use the opposite FP face's flux, which corners feed which inside the
+// zone, which faces leave the mesh -- is done once, on the device, and written
+// as a compact program per (direction, zone), stored in dependency-stage order:
+//
+//   header (uint4, one per work item, same order as the stage items)
+//     x  a*nz + z | lagged << 31        y  cOffSet | numCorner << 28
+//     z  program offset, 16-byte units  w  solve order (3 bits x 8) | length << 24
+//   program (16-byte aligned 32-bit words)
+//     w0  nA | nB << 5 | nE << 10 | nX << 15 | nD << 20
+//     w1  pulls per solve step (2 bits x 8)
+//     corner records  [nC]     {sumArea, Volume}
+//     FP-in entries   [nB+nA]  {upwind | c << 28 | boundary << 31, -Omega.A_fp}
+//     EZ-opp entries  [nB]     {c | cez << 3, Volume/Omega.A_ez}  (pairs FP-in entry i < nB)
+//     EZ entries      [nE]     {c | cez << 3, 0.5 Omega.A_ez}
+//     pulls           [nD]     {n, Omega.A_ez}  solve order; n feeds the step's corner
+//     exits           [nX]     b | c << 28
+//
+// A team of GT lanes runs one program; each lane carries GPL consecutive
+// groups (paired FP32 instructions on group pairs).  Every loop of the program
+// is uniform across the team, so the lanes of one team never diverge, and the
+// teams of one warp differ only in trip counts.  Each lane reads and writes
+// only its own groups of the team's shared arrays, so after the program has
+// been staged no further synchronisation is needed.
+//
+// Memory round trips per zone: (1) header; (2) program, previous flux and
+// source of every corner (asynchronous copies), cross sections; (3) every
+// upwind flux.  The intra-zone solve pulls from upstream corners in the order
+// the reference pushes to downstream ones, so every FMA chain of the solve is
+// the reference's.
+#include "umt_common.cuh"
+#include "sweep32_util.cuh"
+
+#include <algorithm>
+
+namespace umt {
+
+constexpr int P32_NT = 128;
+constexpr int P32_MAXCHUNK = 48;        // 16-byte units: 8 + 8*(8+24+24+24) + 4*24 bytes
+
+struct ProgP {
+  int nz, nc, nb, tstride, bstride;     // tstride: floats per team (Q and S arrays); bstride: program bytes per team
+  const uint4 *hdr;
+  const int *stageOffset, *stageCount;
+  const uint4 *prog;
+  const float *Sigt, *STotal;
+  float tau;
+  const float *psi_old;
+  float *psi_new, *psiB;
+};
+
+template <int NP>
+__device__ __forceinline__ void ldg2(const float *p, float2 (&v)[NP]) {
+  if constexpr (NP == 2) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = make_float2(t.x, t.y); v[1] = make_float2(t.z, t.w);
+  } else {
+    v[0] = *reinterpret_cast<const float2 *>(p);
+  }
+}
+
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+template <int GT, int GPL>
+__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, int stage) {
+  static_assert(GPL == 2 || GPL == 4, "group pairs");
+  constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
+  constexpr int G = GT * GPL;
+  extern __shared__ float4 smem4[];
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const int k = blockIdx.x * TEAMS + team;
+  if (k >= p.stageCount[stage]) return;            // whole teams leave together
+  const unsigned tm = team_mask(GT, tid);
+  const int g0 = lane * GPL;
+  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.tstride;      // [8][G] Q, later solved psi
+  float *sS = sQ + 8 * G;                                                         // [8][G] running source
+  unsigned char *sB = reinterpret_cast<unsigned char *>(smem4) + (size_t)TEAMS * p.tstride * 4 +
+                      (size_t)team * p.bstride;
+  const uint4 h = p.hdr[p.stageOffset[stage] + k];
+  const bool bad = (h.x >> 31) != 0;
+  const uint32_t it = h.x & 0x7fffffffu;
+  const int a = (int)(it / (uint32_t)p.nz);
+  const int z = (int)(it - (uint32_t)a * p.nz);
+  const int c0 = (int)(h.y & 0x0fffffffu), nC = (int)(h.y >> 28);
+  const uint32_t ord = h.w & 0xffffffu;
+  const int nch = (int)(h.w >> 24);
+  const size_t abase = (size_t)a * p.nc;
+  float *psiNew = p.psi_new + abase * G + g0;
+  float *psiBA = p.psiB + (size_t)a * p.nb * G + g0;
+  // ---- round trip 2: program, previous flux, source, cross sections ----
+  {
+    const uint4 *src = p.prog + h.z;
+    for (int e = lane; e < nch; e += GT) cp_async16_cg(sB + 16 * e, src + e);
+    const float *po = p.psi_old + (abase + c0) * G + g0;
+    const float *st = p.STotal + (size_t)c0 * G + g0;
+    for (int c = 0; c < nC; ++c) {
+      cp_async(sQ + c * G + g0, po + (size_t)c * G, GPL * 4);
+      cp_async(sS + c * G + g0, st + (size_t)c * G, GPL * 4);
+    }
+  }
+  float2 sg[NP];
+  ldg2<NP>(p.Sigt + (size_t)z * G + g0, sg);
+  cp_async_wait_all();
+  __syncwarp(tm);
+  const uint32_t *W = reinterpret_cast<const uint32_t *>(sB);
+  const uint32_t cnt = W[0], pcnt = W[1];
+  const int nA = cnt & 31, nB = (cnt >> 5) & 31, nE = (cnt >> 10) & 31, nX = (cnt >> 15) & 31,
+            nD = (cnt >> 20) & 31;
+  const float2 *crec = reinterpret_cast<const float2 *>(sB + 8);
+  const uint2 *fin = reinterpret_cast<const uint2 *>(sB + 8 + 8 * nC);
+  const uint2 *ezo = fin + nB + nA;
+  const uint2 *eze = ezo + nB;
+  const uint2 *pul = eze + nE;
+  const uint32_t *ex = reinterpret_cast<const uint32_t *>(pul + nD);
+  // ---- corner sources: Q = tau*psi_old + STotal, S = V*Q ----
+  const float2 tau2 = f2(p.tau);
+  for (int c = 0; c < nC; ++c) {
+    float2 q[NP], s[NP];
+    ld2<NP>(sQ + c * G + g0, q);
+    ld2<NP>(sS + c * G + g0, s);
+    const float2 v2 = f2(crec[c].y);
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+      q[j] = __ffma2_rn(tau2, q[j], s[j]);
+      s[j] = __fmul2_rn(v2, q[j]);
+    }
+    st2<NP>(sQ + c * G + g0, q);
+    st2<NP>(sS + c * G + g0, s);
+  }
+  // ---- round trip 3: upwind fluxes; FP inflow and the EZ closure that uses them ----
+  const int nF = nA + nB;
+  for (int base = 0; base < nF; base += NFC) {
+    float2 pf[NFC][NP];
+#pragma unroll
+    for (int j = 0; j < NFC; ++j) {
+      if (base + j < nF) {
+        const uint32_t code = fin[base + j].x;
+        const size_t idx = code & 0x0fffffffu;
+        ldg2<NP>(((code >> 31) ? psiBA : psiNew) + idx * G, pf[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NFC; ++j) {
+      const int i = base + j;
+      if (i < nF) {
+        const uint2 e = fin[i];
+        const int c = (e.x >> 28) & 7;
+        const float2 w2 = f2(__uint_as_float(e.y));
+        float2 sc[NP];
+        ld2<NP>(sS + c * G + g0, sc);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) sc[q] = __ffma2_rn(w2, pf[j][q], sc[q]);
+        if (i < nB) {
+          // closure of SweepUCBxyz.F90:219-243 divided through by aez^4: with
+          // x = sigma*V/aez, N = 1.82x^2+4x+3, Dh = 2x^3+3x^2+2x+1,
+          //   sez = V*(N*(sigma*psi_opp - Qc) + Dh*(Qc - Qz)) / (N + 2x*Dh),
+          // x capped at 1e8 so the polynomials stay finite in FP32
+          const uint2 o = ezo[i];
+          const int cez = (o.x >> 3) & 7;
+          const float2 r2 = f2(__uint_as_float(o.y));
+          const float2 V2 = f2(crec[c].y);
+          float2 Qc[NP], Qz[NP], sz[NP];
+          ld2<NP>(sQ + c * G + g0, Qc);
+          ld2<NP>(sQ + cez * G + g0, Qz);
+          ld2<NP>(sS + cez * G + g0, sz);
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            float2 x = __fmul2_rn(sg[q], r2);
+            x.x = fminf(x.x, 1.0e8f); x.y = fminf(x.y, 1.0e8f);
+            const float2 N = __ffma2_rn(__ffma2_rn(f2(1.82f), x, f2(4.f)), x, f2(3.f));
+            const float2 Dh = __ffma2_rn(__ffma2_rn(__ffma2_rn(f2(2.f), x, f2(3.f)), x, f2(2.f)), x, f2(1.f));
+            const float2 den = __ffma2_rn(__fadd2_rn(x, x), Dh, N);
+            const float2 Aq = __ffma2_rn(sg[q], pf[j][q], neg2(Qc[q]));
+            const float2 Bq = __fadd2_rn(Qc[q], neg2(Qz[q]));
+            const float2 num = __ffma2_rn(N, Aq, __fmul2_rn(Dh, Bq));
+            const float2 sez = __fmul2_rn(V2, make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
+            sc[q] = __fadd2_rn(sc[q], sez);
+            sz[q] = __fadd2_rn(sz[q], neg2(sez));
+          }
+          st2<NP>(sS + cez * G + g0, sz);
+        }
+        st2<NP>(sS + c * G + g0, sc);
+      }
+    }
+  }
+  // ---- EZ faces without an incoming opposite FP face: sez = 0.5*aez/sigma*(Qc - Qz) ----
+  if (nE > 0) {
+    float2 rs[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) rs[q] = make_float2(__frcp_rn(sg[q].x), __frcp_rn(sg[q].y));
+    for (int i = 0; i < nE; ++i) {
+      const uint2 o = eze[i];
+      const int c = o.x & 7, cez = (o.x >> 3) & 7;
+      const float2 h2 = f2(__uint_as_float(o.y));
+      float2 Qc[NP], Qz[NP], sc[NP], sz[NP];
+      ld2<NP>(sQ + c * G + g0, Qc);
+      ld2<NP>(sQ + cez * G + g0, Qz);
+      ld2<NP>(sS + c * G + g0, sc);
+      ld2<NP>(sS + cez * G + g0, sz);
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float2 sez = __fmul2_rn(__fmul2_rn(h2, rs[q]), __fadd2_rn(Qc[q], neg2(Qz[q])));
+        sc[q] = __fadd2_rn(sc[q], sez);
+        sz[q] = __fadd2_rn(sz[q], neg2(sez));
+      }
+      st2<NP>(sS + c * G + g0, sc);
+      st2<NP>(sS + cez * G + g0, sz);
+    }
+  }
+  // ---- corner solve; a lagged zone (SweepUCBxyz.F90:283-297) takes its
+  //      upstream terms from the previous values of its corners ----
+  if (bad) {
+    for (int c = 0; c < nC; ++c) {
+      float2 old[NP];
+      ldg2<NP>(psiNew + (size_t)(c0 + c) * G, old);
+      st2<NP>(sQ + c * G + g0, old);
+    }
+  }
+  float *res = bad ? sS : sQ;                      // where solved corners are kept
+  int dp = 0;
+  for (int i = 0; i < nC; ++i) {
+    const int c = (int)((ord >> (3 * i)) & 7u);
+    const int np = (int)((pcnt >> (2 * i)) & 3u);
+    float2 acc[NP];
+    ld2<NP>(sS + c * G + g0, acc);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (j < np) {
+        const uint2 d = pul[dp + j];
+        const float2 ae = f2(__uint_as_float(d.y));
+        float2 pn[NP];
+        ld2<NP>(sQ + (int)(d.x & 7u) * G + g0, pn);
+#pragma unroll
+        for (int q = 0; q < NP; ++q) acc[q] = __ffma2_rn(ae, pn[q], acc[q]);
+      }
+    }
+    dp += np;
+    const float2 cr = crec[c];
+    float2 v[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const float2 dn = __ffma2_rn(sg[q], f2(cr.y), f2(cr.x));
+      v[q] = make_float2(__fdividef(acc[q].x, dn.x), __fdividef(acc[q].y, dn.y));
+    }
+    st2<NP>(res + c * G + g0, v);
+    st2<NP>(psiNew + (size_t)(c0 + c) * G, v);
+  }
+  for (int x = 0; x < nX; ++x) {
+    const uint32_t e = ex[x];
+    float2 v[NP];
+    ld2<NP>(res + (int)((e >> 28) & 7u) * G + g0, v);
+    st2<NP>(psiBA + (size_t)(e & 0x0fffffffu) * G, v);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Program builder: one thread per work item, run twice (sizes, then contents).
+// ---------------------------------------------------------------------------
+constexpr unsigned PROG_ERR_RANGE = 1u;       // an index does not fit its field
+constexpr unsigned PROG_ERR_PULLS = 2u;       // more than 3 upstream corners feed one corner
+constexpr unsigned PROG_ERR_ORDER = 4u;       // solve order is not a permutation
+constexpr unsigned PROG_ERR_TOTAL = 8u;       // programs exceed 2^32 16-byte units
+
+__device__ __forceinline__ float pick3(const float4 &v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+__device__ __forceinline__ int pick3i(const int4 &v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+
+// Returns the program length in 16-byte units; writes it when `out` is set.
+__device__ int prog_item(uint2 w, uint32_t ordNib, int nz, int nc, const float4 *rec, const int4 *conn,
+                         uint32_t *out, uint32_t *ord3, unsigned *err) {
+  const bool bad = (w.x >> 31) != 0;
+  const uint32_t it = w.x & 0x7fffffffu;
+  const int a = (int)(it / (uint32_t)nz);
+  const int c0 = (int)(w.y & 0x0fffffffu), nC = (int)(w.y >> 28);
+  float4 r0[UMT_MAXCORNER], r1[UMT_MAXCORNER];
+  int4 cn[UMT_MAXCORNER];
+  int ncf[UMT_MAXCORNER];
+  for (int c = 0; c < nC; ++c) {
+    const size_t i = ((size_t)a * nc + c0 + c) * 2;
+    r0[c] = rec[i];
+    r1[c] = rec[i + 1];
+    cn[c] = conn[c0 + c];
+    ncf[c] = cn[c].w >> 9;
+  }
+  int ordc[UMT_MAXCORNER];
+  unsigned seen = 0;
+  for (int i = 0; i < nC; ++i) {
+    ordc[i] = bad ? i : (int)((ordNib >> (4 * i)) & 15u);
+    if (ordc[i] >= nC || ((seen >> ordc[i]) & 1u)) { atomicOr(err, PROG_ERR_ORDER); ordc[i] = i; }
+    seen |= 1u << ordc[i];
+  }
+  auto cezOf = [&](int c, int e) { return (cn[c].w >> (3 * e)) & 7; };
+  auto isB = [&](int c, int f) {          // incoming FP face f whose partner EZ face carries flux
+    const int e = f == 0 ? 2 : f - 1;
+    return ncf[c] == 3 && pick3(r1[c], e) > 0.f;
+  };
+  int nA = 0, nB = 0, nE = 0, nX = 0, nD = 0;
+  uint32_t pc = 0;
+  for (int c = 0; c < nC; ++c)
+    for (int f = 0; f < ncf[c]; ++f) {
+      const float af = pick3(r0[c], f);
+      if (af < 0.f) { if (isB(c, f)) ++nB; else ++nA; }
+      if (pick3i(cn[c], f) < 0 && af > 0.f) ++nX;
+      const float ae = pick3(r1[c], f);
+      const int fo = f == 2 ? 0 : f + 1;
+      if (ae > 0.f && !(ncf[c] == 3 && pick3(r0[c], fo) < 0.f)) ++nE;
+    }
+  for (int i = 0; i < nC; ++i) {
+    const int t = ordc[i];
+    int k = 0;
+    for (int j = 0; j < nC; ++j) {
+      if (!bad && j >= i) break;
+      const int n = ordc[j];
+      if (n == t) continue;
+      for (int e = 0; e < ncf[n]; ++e)
+        if (pick3(r1[n], e) > 0.f && cezOf(n, e) == t) ++k;
+    }
+    if (k > 3) { atomicOr(err, PROG_ERR_PULLS); k = 3; }
+    pc |= (uint32_t)k << (2 * i);
+    nD += k;
+  }
+  const int words = 2 + 2 * nC + 2 * (nA + nB) + 2 * nB + 2 * nE + 2 * nD + nX;
+  const int chunks = (words * 4 + 15) / 16;
+  if (!out) return chunks;
+  uint32_t o = 0;
+  out[o++] = (uint32_t)nA | (uint32_t)nB << 5 | (uint32_t)nE << 10 | (uint32_t)nX << 15 | (uint32_t)nD << 20;
+  out[o++] = pc;
+  for (int c = 0; c < nC; ++c) { out[o++] = __float_as_uint(r0[c].w); out[o++] = __float_as_uint(r1[c].w); }
+  auto upcode = [&](int c, int f) -> uint32_t {
+    const int up = pick3i(cn[c], f);
+    const uint32_t idx = up >= 0 ? (uint32_t)up : (uint32_t)(-up - 1);
+    if (idx > 0x0fffffffu) atomicOr(err, PROG_ERR_RANGE);
+    return (idx & 0x0fffffffu) | (uint32_t)c << 28 | (up < 0 ? 0x80000000u : 0u);
+  };
+  const uint32_t oB = o, oA = o + 2 * nB, oEo = o + 2 * (nA + nB);
+  uint32_t ib = 0, ia = 0;
+  for (int c = 0; c < nC; ++c)
+    for (int f = 0; f < ncf[c]; ++f) {
+      const float af = pick3(r0[c], f);
+      if (!(af < 0.f)) continue;
+      if (isB(c, f)) {
+        const int e = f == 0 ? 2 : f - 1;
+        out[oB + 2 * ib] = upcode(c, f);
+        out[oB + 2 * ib + 1] = __float_as_uint(-af);
+        out[oEo + 2 * ib] = (uint32_t)c | (uint32_t)cezOf(c, e) << 3;
+        out[oEo + 2 * ib + 1] = __float_as_uint(r1[c].w * __frcp_rn(pick3(r1[c], e)));
+        ++ib;
+      } else {
+        out[oA + 2 * ia] = upcode(c, f);
+        out[oA + 2 * ia + 1] = __float_as_uint(-af);
+        ++ia;
+      }
+    }
+  o = oEo + 2 * nB;
+  for (int c = 0; c < nC; ++c)
+    for (int e = 0; e < ncf[c]; ++e) {
+      const float ae = pick3(r1[c], e);
+      const int fo = e == 2 ? 0 : e + 1;
+      if (ae > 0.f && !(ncf[c] == 3 && pick3(r0[c], fo) < 0.f)) {
+        out[o++] = (uint32_t)c | (uint32_t)cezOf(c, e) << 3;
+        out[o++] = __float_as_uint(0.5f * ae);
+      }
+    }
+  for (int i = 0; i < nC; ++i) {
+    const int t = ordc[i];
+    int k = 0;
+    for (int j = 0; j < nC && k < 3; ++j) {
+      if (!bad && j >= i) break;
+      const int n = ordc[j];
+      if (n == t) continue;
+      for (int e = 0; e < ncf[n] && k < 3; ++e)
+        if (pick3(r1[n], e) > 0.f && cezOf(n, e) == t) {
+          out[o++] = (uint32_t)n;
+          out[o++] = __float_as_uint(pick3(r1[n], e));
+          ++k;
+        }
+    }
+  }
+  for (int c = 0; c < nC; ++c)
+    for (int f = 0; f < ncf[c]; ++f) {
+      const int up = pick3i(cn[c], f);
+      if (up < 0 && pick3(r0[c], f) > 0.f) {
+        const uint32_t b = (uint32_t)(-up - 1);
+        if (b > 0x0fffffffu) atomicOr(err, PROG_ERR_RANGE);
+        out[o++] = (b & 0x0fffffffu) | (uint32_t)c << 28;
+      }
+    }
+  while (o < (uint32_t)chunks * 4) out[o++] = 0u;
+  uint32_t o3 = 0;
+  for (int i = 0; i < nC; ++i) o3 |= (uint32_t)ordc[i] << (3 * i);
+  *ord3 = o3;
+  return chunks;
+}
+
+__global__ void k_prog_sizes(long long n, const uint2 *items2, const uint32_t *order, int nz, int nc,
+                             const float4 *rec, const int4 *conn, uint32_t *sizes, unsigned *err,
+                             unsigned *maxch) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const uint2 w = items2[t];
+    uint32_t o3 = 0;
+    const int ch = prog_item(w, order[w.x & 0x7fffffffu], nz, nc, rec, conn, nullptr, &o3, err);
+    sizes[t] = (uint32_t)ch;
+    atomicMax(maxch, (unsigned)ch);
+  }
+}
+
+__global__ void k_prog_write(long long n, const uint2 *items2, const uint32_t *order, int nz, int nc,
+                             const float4 *rec, const int4 *conn, const uint32_t *offs, uint4 *prog, uint4 *hdr,
+                             unsigned *err) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const uint2 w = items2[t];
+    uint32_t o3 = 0;
+    const uint32_t off = offs[t];
+    const int ch = prog_item(w, order[w.x & 0x7fffffffu], nz, nc, rec, conn,
+                             reinterpret_cast<uint32_t *>(prog + off), &o3, err);
+    hdr[t] = make_uint4(w.x, w.y, off, o3 | (uint32_t)ch << 24);
+  }
+}
+
+// Exclusive scan of 32-bit program lengths into 32-bit offsets, in place:
+// per-block scans, a single-block scan of the block totals, then the add.
+constexpr int SCAN_NT = 1024;
+
+__device__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long *total) {
+  __shared__ unsigned long long ws[SCAN_NT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long s = lane < SCAN_NT / 32 ? ws[lane] : 0ull;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < SCAN_NT / 32) ws[lane] = s;
+  }
+  __syncthreads();
+  const unsigned long long incl = x + (w > 0 ? ws[w - 1] : 0ull);
+  *total = ws[SCAN_NT / 32 - 1];
+  __syncthreads();
+  return incl - v;
+}
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_local(long long n, uint32_t *v, unsigned long long *bsum) {
+  const long long i = blockIdx.x * (long long)SCAN_NT + threadIdx.x;
+  const unsigned long long x = i < n ? v[i] : 0u;
+  unsigned long long tot = 0;
+  const unsigned long long ex = block_exclusive_scan(x, &tot);
+  if (i < n) v[i] = (uint32_t)ex;
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_NT) k_scan_totals(long long nb, unsigned long long *bsum) {
+  unsigned long long carry = 0;
+  for (long long base = 0; base < nb; base += SCAN_NT) {
+    const long long i = base + threadIdx.x;
+    const unsigned long long x = i < nb ? bsum[i] : 0ull;
+    unsigned long long tot = 0;
+    const unsigned long long ex = block_exclusive_scan(x, &tot);
+    if (i < nb) bsum[i] = ex + carry;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) bsum[nb] = carry;
+}
+
+__global__ void k_scan_add(long long n, uint32_t *v, const unsigned long long *bsum, unsigned *err) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long o = bsum[i / SCAN_NT] + v[i];
+    if (o > 0xffffffffull) atomicOr(err, PROG_ERR_TOTAL);
+    v[i] = (uint32_t)o;
+  }
+}
+
+bool sweep32p_supported(int G, int GT, int GPL) {
+  return GT * GPL == G && (GPL == 2 || GPL == 4) &&
+         (GT == 1 || GT == 2 || GT == 4 || GT == 8 || GT == 16 || GT == 32);
+}
+
+static int team_stride_p(int G) {
+  // 16*G floats (Q and S), padded so that consecutive teams start 8 banks apart
+  const int base = 16 * G;
+  return base + ((8 - base % 32) % 32 + 32) % 32;
+}
+
+// Build the zone programs of every work item (once per context, outside any
+// stream capture).  On a geometry the program format cannot hold, the context
+// keeps no programs and the FP32 sweep uses the corner-slot kernel.
+int prepare_prog32(Ctx &c) {
+  if (c.progState != 0) return 0;
+  c.progState = -1;
+  const long long n = (long long)c.A * c.nz;
+  if (n <= 0 || n > 0x7fffffffll || c.nc > 0x0fffffff || c.nb > 0x0fffffff) return 0;
+  uint32_t *offs = nullptr;
+  unsigned long long *bsum = nullptr;
+  unsigned *flags = nullptr;                       // [0] error bits, [1] longest program
+  const long long nb = (n + SCAN_NT - 1) / SCAN_NT;
+  auto cleanup = [&]() {
+    if (offs) cudaFree(offs);
+    if (bsum) cudaFree(bsum);
+    if (flags) cudaFree(flags);
+  };
+  if (cudaMalloc((void **)&offs, (size_t)n * 4) != cudaSuccess ||
+      cudaMalloc((void **)&bsum, (size_t)(nb + 1) * 8) != cudaSuccess ||
+      cudaMalloc((void **)&flags, 8) != cudaSuccess) {
+    cleanup();
+    cudaGetLastError();
+    return 0;                                      // no room for programs: corner-slot kernel
+  }
+  UMT_CUDA(cudaMemsetAsync(flags, 0, 8, c.stream));
+  const int grid = 152 * 8;
+  k_prog_sizes<<<grid, 256, 0, c.stream>>>(n, c.sch.items2, c.sch.order, c.nz, c.nc, (const float4 *)c.rec32,
+                                           (const int4 *)c.conn32, offs, flags, flags + 1);
+  k_scan_local<<<(unsigned)nb, SCAN_NT, 0, c.stream>>>(n, offs, bsum);
+  k_scan_totals<<<1, SCAN_NT, 0, c.stream>>>(nb, bsum);
+  k_scan_add<<<grid, 256, 0, c.stream>>>(n, offs, bsum, flags);
+  unsigned long long total = 0;
+  unsigned hf[2] = {0, 0};
+  UMT_CUDA(cudaMemcpyAsync(&total, bsum + nb, 8, cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  UMT_CUDA(cudaGetLastError());
+  if (hf[0] != 0 || hf[1] > (unsigned)P32_MAXCHUNK || total == 0) { cleanup(); return 0; }
+  if (cudaMalloc((void **)&c.prog32, (size_t)total * 16) != cudaSuccess ||
+      cudaMalloc((void **)&c.hdr32, (size_t)n * 16) != cudaSuccess) {
+    if (c.prog32) cudaFree(c.prog32);
+    if (c.hdr32) cudaFree(c.hdr32);
+    c.prog32 = nullptr; c.hdr32 = nullptr;
+    cleanup();
+    cudaGetLastError();
+    return 0;
+  }
+  k_prog_write<<<grid, 256, 0, c.stream>>>(n, c.sch.items2, c.sch.order, c.nz, c.nc, (const float4 *)c.rec32,
+                                           (const int4 *)c.conn32, offs, (uint4 *)c.prog32, (uint4 *)c.hdr32,
+                                           flags);
+  UMT_CUDA(cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  UMT_CUDA(cudaGetLastError());
+  cleanup();
+  if (hf[0] != 0) {
+    cudaFree(c.prog32); cudaFree(c.hdr32);
+    c.prog32 = nullptr; c.hdr32 = nullptr;
+    return 0;
+  }
+  c.progBytes = (size_t)total * 16;
+  c.progMaxChunks = (int)hf[1];
+#define UMT_ATTRP(gt, gpl) TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl>));
+#define TRY_RC_P(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
+  UMT_ATTRP(1, 2) UMT_ATTRP(2, 2) UMT_ATTRP(4, 2) UMT_ATTRP(8, 2) UMT_ATTRP(16, 2) UMT_ATTRP(32, 2)
+  UMT_ATTRP(1, 4) UMT_ATTRP(2, 4) UMT_ATTRP(4, 4) UMT_ATTRP(8, 4) UMT_ATTRP(16, 4) UMT_ATTRP(32, 4)
+#undef UMT_ATTRP
+#undef TRY_RC_P
+  c.progState = 1;
+  return 0;
+}
+
+// One launch per dependency stage.  Returns 1 when the tile or the context
+// has no program kernel (the caller then uses the corner-slot kernel).
+int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
+  if (c.progState != 1 || !sweep32p_supported(c.G, GT, GPL)) return 1;
+  ProgP p;
+  p.nz = c.nz; p.nc = c.nc; p.nb = c.nb;
+  p.tstride = team_stride_p(c.G);
+  p.bstride = c.progMaxChunks * 16;
+  p.hdr = (const uint4 *)c.hdr32; p.prog = (const uint4 *)c.prog32;
+  p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
+  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
+  p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
+  const int TEAMS = P32_NT / GT;
+  const size_t smem = (size_t)TEAMS * ((size_t)p.tstride * 4 + p.bstride);
+#define UMT_LAUNCHP(gt, gpl)                                                                   \
+  if (GT == gt && GPL == gpl) {                                                                \
+    for (int s = 0; s < c.sch.nStages; ++s) {                                                  \
+      const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                \
+      k_sweep32p<gt, gpl><<<blocks, P32_NT, smem, c.stream>>>(p, s);                           \
+    }                                                                                          \
+    UMT_CUDA(cudaGetLastError());                                                              \
+    return 0;                                                                                  \
+  }
+  UMT_LAUNCHP(1, 2) UMT_LAUNCHP(2, 2) UMT_LAUNCHP(4, 2) UMT_LAUNCHP(8, 2) UMT_LAUNCHP(16, 2) UMT_LAUNCHP(32, 2)
+  UMT_LAUNCHP(1, 4) UMT_LAUNCHP(2, 4) UMT_LAUNCHP(4, 4) UMT_LAUNCHP(8, 4) UMT_LAUNCHP(16, 4) UMT_LAUNCHP(32, 4)
+#undef UMT_LAUNCHP
+  return 1;
+}
+
+}  // namespace umt

@@ -65,8 +65,14 @@ struct Ctx {
   float *vol32 = nullptr;                       // [nc]
   bool rec32Ready = false;
   int tileGT = 0, tileGPL = 0;                  // FP32 group tile (0: choose)
-  int sweepMode = 0;                            // FP32: 0 = one launch per stage, 1 = persistent
+  int sweepMode = 0;                            // FP32 kernel choice (umt103_set_sweep_mode)
   bool useCompact = true;                       // FP32: compact-list kernel where the tile allows
+  // zone programs of the FP32 program kernel (sweep32p.cu)
+  void *prog32 = nullptr;                       // programs, 16-byte units
+  void *hdr32 = nullptr;                        // [A*nz] uint4 headers in stage order
+  size_t progBytes = 0;
+  int progMaxChunks = 0;                        // longest program, 16-byte units
+  int progState = 0;                            // 0 not built, 1 built, -1 unavailable
   int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
   int *ticket = nullptr;                        // persistent-mode work ticket
   Schedule sch;
@@ -146,5 +152,9 @@ int prepare_sweep32(Ctx &c);
 bool sweep32_supported(int G, int GT, int GPL);
 int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL);
 void default_tile(int G, int *GT, int *GPL);
+// zone-program FP32 kernel (sweep32p.cu)
+int prepare_prog32(Ctx &c);
+bool sweep32p_supported(int G, int GT, int GPL);
+int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL);
 
 }  // namespace umt
