@@ -36,6 +36,7 @@
 // the reference's.
 #include "umt_common.cuh"
 #include "sweep32_util.cuh"
+#include "../../include/umt103.h"
 
 #include <algorithm>
 
@@ -67,6 +68,21 @@ __device__ __forceinline__ void ldg2(const float *p, float2 (&v)[NP]) {
 
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
+// a / b for positive, normal b: the hardware reciprocal approximation
+// (rcp.approx.ftz.f32, max. 1 ulp) times a, one paired multiply per group pair.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float2 div2(float2 a, float2 b) {
+  return __fmul2_rn(a, make_float2(rcp_approx(b.x), rcp_approx(b.y)));
+}
+
+// Floats between rows c and c+1 of one array: Q and S rows interleaved, the
+// pair padded to a whole number of 32-bank spans.
+__host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 * 32; }
+
 template <int GT, int GPL>
 __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, int stage) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
@@ -78,8 +94,13 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
   if (k >= p.stageCount[stage]) return;            // whole teams leave together
   const unsigned tm = team_mask(GT, tid);
   const int g0 = lane * GPL;
-  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.tstride;      // [8][G] Q, later solved psi
-  float *sS = sQ + 8 * G;                                                         // [8][G] running source
+  // Row c of Q (later the solved psi) at c*RP, row c of S (running source) at
+  // c*RP + G: a team's window of one row lies in the same banks whatever the
+  // corner, and consecutive teams are G banks apart (team stride), so the
+  // teams sharing a shared-memory wavefront never collide.
+  constexpr int RP = pair_stride(G);
+  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.tstride;
+  float *sS = sQ + G;
   unsigned char *sB = reinterpret_cast<unsigned char *>(smem4) + (size_t)TEAMS * p.tstride * 4 +
                       (size_t)team * p.bstride;
   const uint4 h = p.hdr[p.stageOffset[stage] + k];
@@ -100,8 +121,8 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
     const float *po = p.psi_old + (abase + c0) * G + g0;
     const float *st = p.STotal + (size_t)c0 * G + g0;
     for (int c = 0; c < nC; ++c) {
-      cp_async(sQ + c * G + g0, po + (size_t)c * G, GPL * 4);
-      cp_async(sS + c * G + g0, st + (size_t)c * G, GPL * 4);
+      cp_async(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4);
+      cp_async(sS + c * RP + g0, st + (size_t)c * G, GPL * 4);
     }
   }
   float2 sg[NP];
@@ -122,16 +143,16 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
   const float2 tau2 = f2(p.tau);
   for (int c = 0; c < nC; ++c) {
     float2 q[NP], s[NP];
-    ld2<NP>(sQ + c * G + g0, q);
-    ld2<NP>(sS + c * G + g0, s);
+    ld2<NP>(sQ + c * RP + g0, q);
+    ld2<NP>(sS + c * RP + g0, s);
     const float2 v2 = f2(crec[c].y);
 #pragma unroll
     for (int j = 0; j < NP; ++j) {
       q[j] = __ffma2_rn(tau2, q[j], s[j]);
       s[j] = __fmul2_rn(v2, q[j]);
     }
-    st2<NP>(sQ + c * G + g0, q);
-    st2<NP>(sS + c * G + g0, s);
+    st2<NP>(sQ + c * RP + g0, q);
+    st2<NP>(sS + c * RP + g0, s);
   }
   // ---- round trip 3: upwind fluxes; FP inflow and the EZ closure that uses them ----
   const int nF = nA + nB;
@@ -153,7 +174,7 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
         const int c = (e.x >> 28) & 7;
         const float2 w2 = f2(__uint_as_float(e.y));
         float2 sc[NP];
-        ld2<NP>(sS + c * G + g0, sc);
+        ld2<NP>(sS + c * RP + g0, sc);
 #pragma unroll
         for (int q = 0; q < NP; ++q) sc[q] = __ffma2_rn(w2, pf[j][q], sc[q]);
         if (i < nB) {
@@ -166,9 +187,9 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
           const float2 r2 = f2(__uint_as_float(o.y));
           const float2 V2 = f2(crec[c].y);
           float2 Qc[NP], Qz[NP], sz[NP];
-          ld2<NP>(sQ + c * G + g0, Qc);
-          ld2<NP>(sQ + cez * G + g0, Qz);
-          ld2<NP>(sS + cez * G + g0, sz);
+          ld2<NP>(sQ + c * RP + g0, Qc);
+          ld2<NP>(sQ + cez * RP + g0, Qz);
+          ld2<NP>(sS + cez * RP + g0, sz);
 #pragma unroll
           for (int q = 0; q < NP; ++q) {
             float2 x = __fmul2_rn(sg[q], r2);
@@ -179,13 +200,13 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
             const float2 Aq = __ffma2_rn(sg[q], pf[j][q], neg2(Qc[q]));
             const float2 Bq = __fadd2_rn(Qc[q], neg2(Qz[q]));
             const float2 num = __ffma2_rn(N, Aq, __fmul2_rn(Dh, Bq));
-            const float2 sez = __fmul2_rn(V2, make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
+            const float2 sez = __fmul2_rn(V2, div2(num, den));
             sc[q] = __fadd2_rn(sc[q], sez);
             sz[q] = __fadd2_rn(sz[q], neg2(sez));
           }
-          st2<NP>(sS + cez * G + g0, sz);
+          st2<NP>(sS + cez * RP + g0, sz);
         }
-        st2<NP>(sS + c * G + g0, sc);
+        st2<NP>(sS + c * RP + g0, sc);
       }
     }
   }
@@ -199,18 +220,18 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
       const int c = o.x & 7, cez = (o.x >> 3) & 7;
       const float2 h2 = f2(__uint_as_float(o.y));
       float2 Qc[NP], Qz[NP], sc[NP], sz[NP];
-      ld2<NP>(sQ + c * G + g0, Qc);
-      ld2<NP>(sQ + cez * G + g0, Qz);
-      ld2<NP>(sS + c * G + g0, sc);
-      ld2<NP>(sS + cez * G + g0, sz);
+      ld2<NP>(sQ + c * RP + g0, Qc);
+      ld2<NP>(sQ + cez * RP + g0, Qz);
+      ld2<NP>(sS + c * RP + g0, sc);
+      ld2<NP>(sS + cez * RP + g0, sz);
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const float2 sez = __fmul2_rn(__fmul2_rn(h2, rs[q]), __fadd2_rn(Qc[q], neg2(Qz[q])));
         sc[q] = __fadd2_rn(sc[q], sez);
         sz[q] = __fadd2_rn(sz[q], neg2(sez));
       }
-      st2<NP>(sS + c * G + g0, sc);
-      st2<NP>(sS + cez * G + g0, sz);
+      st2<NP>(sS + c * RP + g0, sc);
+      st2<NP>(sS + cez * RP + g0, sz);
     }
   }
   // ---- corner solve; a lagged zone (SweepUCBxyz.F90:283-297) takes its
@@ -219,7 +240,7 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
     for (int c = 0; c < nC; ++c) {
       float2 old[NP];
       ldg2<NP>(psiNew + (size_t)(c0 + c) * G, old);
-      st2<NP>(sQ + c * G + g0, old);
+      st2<NP>(sQ + c * RP + g0, old);
     }
   }
   float *res = bad ? sS : sQ;                      // where solved corners are kept
@@ -228,14 +249,14 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
     const int c = (int)((ord >> (3 * i)) & 7u);
     const int np = (int)((pcnt >> (2 * i)) & 3u);
     float2 acc[NP];
-    ld2<NP>(sS + c * G + g0, acc);
+    ld2<NP>(sS + c * RP + g0, acc);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       if (j < np) {
         const uint2 d = pul[dp + j];
         const float2 ae = f2(__uint_as_float(d.y));
         float2 pn[NP];
-        ld2<NP>(sQ + (int)(d.x & 7u) * G + g0, pn);
+        ld2<NP>(sQ + (int)(d.x & 7u) * RP + g0, pn);
 #pragma unroll
         for (int q = 0; q < NP; ++q) acc[q] = __ffma2_rn(ae, pn[q], acc[q]);
       }
@@ -246,15 +267,15 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
 #pragma unroll
     for (int q = 0; q < NP; ++q) {
       const float2 dn = __ffma2_rn(sg[q], f2(cr.y), f2(cr.x));
-      v[q] = make_float2(__fdividef(acc[q].x, dn.x), __fdividef(acc[q].y, dn.y));
+      v[q] = div2(acc[q], dn);
     }
-    st2<NP>(res + c * G + g0, v);
+    st2<NP>(res + c * RP + g0, v);
     st2<NP>(psiNew + (size_t)(c0 + c) * G, v);
   }
   for (int x = 0; x < nX; ++x) {
     const uint32_t e = ex[x];
     float2 v[NP];
-    ld2<NP>(res + (int)((e >> 28) & 7u) * G + g0, v);
+    ld2<NP>(res + (int)((e >> 28) & 7u) * RP + g0, v);
     st2<NP>(psiBA + (size_t)(e & 0x0fffffffu) * G, v);
   }
 }
@@ -270,9 +291,11 @@ constexpr unsigned PROG_ERR_TOTAL = 8u;       // programs exceed 2^32 16-byte un
 __device__ __forceinline__ float pick3(const float4 &v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 __device__ __forceinline__ int pick3i(const int4 &v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
 
-// Returns the program length in 16-byte units; writes it when `out` is set.
+// Returns the program length in 16-byte units and the program's shape (every
+// count and trip count the kernel's loops depend on); writes the program
+// when `out` is set.
 __device__ int prog_item(uint2 w, uint32_t ordNib, int nz, int nc, const float4 *rec, const int4 *conn,
-                         uint32_t *out, uint32_t *ord3, unsigned *err) {
+                         uint32_t *out, uint32_t *ord3, unsigned long long *shape, unsigned *err) {
   const bool bad = (w.x >> 31) != 0;
   const uint32_t it = w.x & 0x7fffffffu;
   const int a = (int)(it / (uint32_t)nz);
@@ -326,9 +349,13 @@ __device__ int prog_item(uint2 w, uint32_t ordNib, int nz, int nc, const float4 
   }
   const int words = 2 + 2 * nC + 2 * (nA + nB) + 2 * nB + 2 * nE + 2 * nD + nX;
   const int chunks = (words * 4 + 15) / 16;
+  const uint32_t counts =
+      (uint32_t)nA | (uint32_t)nB << 5 | (uint32_t)nE << 10 | (uint32_t)nX << 15 | (uint32_t)nD << 20;
+  *shape = (unsigned long long)counts | (unsigned long long)pc << 25 | (unsigned long long)nC << 41 |
+           (unsigned long long)bad << 45;
   if (!out) return chunks;
   uint32_t o = 0;
-  out[o++] = (uint32_t)nA | (uint32_t)nB << 5 | (uint32_t)nE << 10 | (uint32_t)nX << 15 | (uint32_t)nD << 20;
+  out[o++] = counts;
   out[o++] = pc;
   for (int c = 0; c < nC; ++c) { out[o++] = __float_as_uint(r0[c].w); out[o++] = __float_as_uint(r1[c].w); }
   auto upcode = [&](int c, int f) -> uint32_t {
@@ -397,28 +424,53 @@ __device__ int prog_item(uint2 w, uint32_t ordNib, int nz, int nc, const float4 
   return chunks;
 }
 
+// Items of one stage are independent, so their headers may be stored in any
+// order within the stage.  They are grouped by program shape (hashed into
+// PROG_BINS bins per stage), so that the teams of one warp mostly run programs
+// with identical trip counts and take the same branches.
+constexpr int PROG_BINS = 64;
+
+__device__ __forceinline__ int shape_bin(unsigned long long shape) {
+  return (int)((shape * 0x9E3779B97F4A7C15ull) >> 58);
+}
+
+__device__ __forceinline__ int stage_of(long long t, const int *stageOffset, int nStages) {
+  int lo = 0, hi = nStages - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (stageOffset[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 __global__ void k_prog_sizes(long long n, const uint2 *items2, const uint32_t *order, int nz, int nc,
-                             const float4 *rec, const int4 *conn, uint32_t *sizes, unsigned *err,
-                             unsigned *maxch) {
+                             const float4 *rec, const int4 *conn, const int *stageOffset, int nStages,
+                             uint32_t *sizes, int *binCount, unsigned *err, unsigned *maxch) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const uint2 w = items2[t];
     uint32_t o3 = 0;
-    const int ch = prog_item(w, order[w.x & 0x7fffffffu], nz, nc, rec, conn, nullptr, &o3, err);
+    unsigned long long shape = 0;
+    const int ch = prog_item(w, order[w.x & 0x7fffffffu], nz, nc, rec, conn, nullptr, &o3, &shape, err);
     sizes[t] = (uint32_t)ch;
     atomicMax(maxch, (unsigned)ch);
+    atomicAdd(binCount + (size_t)stage_of(t, stageOffset, nStages) * PROG_BINS + shape_bin(shape), 1);
   }
 }
 
 __global__ void k_prog_write(long long n, const uint2 *items2, const uint32_t *order, int nz, int nc,
-                             const float4 *rec, const int4 *conn, const uint32_t *offs, uint4 *prog, uint4 *hdr,
+                             const float4 *rec, const int4 *conn, const int *stageOffset, int nStages,
+                             const uint32_t *offs, const int *binStart, int *binFill, uint4 *prog, uint4 *hdr,
                              unsigned *err) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const uint2 w = items2[t];
     uint32_t o3 = 0;
+    unsigned long long shape = 0;
     const uint32_t off = offs[t];
     const int ch = prog_item(w, order[w.x & 0x7fffffffu], nz, nc, rec, conn,
-                             reinterpret_cast<uint32_t *>(prog + off), &o3, err);
-    hdr[t] = make_uint4(w.x, w.y, off, o3 | (uint32_t)ch << 24);
+                             reinterpret_cast<uint32_t *>(prog + off), &o3, &shape, err);
+    const size_t bin = (size_t)stage_of(t, stageOffset, nStages) * PROG_BINS + shape_bin(shape);
+    const int dst = binStart[bin] + atomicAdd(binFill + bin, 1);
+    hdr[dst] = make_uint4(w.x, w.y, off, o3 | (uint32_t)ch << 24);
   }
 }
 
@@ -486,10 +538,17 @@ bool sweep32p_supported(int G, int GT, int GPL) {
          (GT == 1 || GT == 2 || GT == 4 || GT == 8 || GT == 16 || GT == 32);
 }
 
-static int team_stride_p(int G) {
-  // 16*G floats (Q and S), padded so that consecutive teams start 8 banks apart
-  const int base = 16 * G;
-  return base + ((8 - base % 32) % 32 + 32) % 32;
+// Floats per team: 8 row pairs, plus G so that consecutive teams start G
+// banks apart (a team's row window is G words wide).
+static int team_stride_p(int G) { return 8 * pair_stride(G) + G; }
+
+// Program bytes staged per team: the longest program, rounded so that the
+// teams' copies start 4 banks apart (entry reads of the teams of one warp are
+// 4 different addresses).
+static int blob_stride_p(int maxChunks) {
+  int ch = maxChunks;
+  while ((4 * ch) % 32 != 4) ++ch;
+  return ch * 16;
 }
 
 // Build the zone programs of every work item (once per context, outside any
@@ -500,36 +559,63 @@ int prepare_prog32(Ctx &c) {
   c.progState = -1;
   const long long n = (long long)c.A * c.nz;
   if (n <= 0 || n > 0x7fffffffll || c.nc > 0x0fffffff || c.nb > 0x0fffffff) return 0;
+  const int nS = c.sch.nStages;
+  if (nS <= 0 || (int)c.sch.hOffset.size() < nS || (int)c.sch.hCount.size() < nS) return 0;
   uint32_t *offs = nullptr;
   unsigned long long *bsum = nullptr;
   unsigned *flags = nullptr;                       // [0] error bits, [1] longest program
+  int *bins = nullptr;                             // [2][nS][PROG_BINS] start, fill
   const long long nb = (n + SCAN_NT - 1) / SCAN_NT;
+  const size_t nbin = (size_t)nS * PROG_BINS;
   auto cleanup = [&]() {
     if (offs) cudaFree(offs);
     if (bsum) cudaFree(bsum);
     if (flags) cudaFree(flags);
+    if (bins) cudaFree(bins);
+    offs = nullptr; bsum = nullptr; flags = nullptr; bins = nullptr;
   };
   if (cudaMalloc((void **)&offs, (size_t)n * 4) != cudaSuccess ||
       cudaMalloc((void **)&bsum, (size_t)(nb + 1) * 8) != cudaSuccess ||
-      cudaMalloc((void **)&flags, 8) != cudaSuccess) {
+      cudaMalloc((void **)&flags, 8) != cudaSuccess ||
+      cudaMalloc((void **)&bins, 2 * nbin * sizeof(int)) != cudaSuccess) {
     cleanup();
     cudaGetLastError();
     return 0;                                      // no room for programs: corner-slot kernel
   }
-  UMT_CUDA(cudaMemsetAsync(flags, 0, 8, c.stream));
+  unsigned long long total = 0;
+  unsigned hf[2] = {0, 0};
+  std::vector<int> hb(nbin);
   const int grid = 152 * 8;
+  auto fail = [&](cudaError_t e, const char *what) {
+    cleanup();
+    return set_error(UMT_ERR_CUDA, "zone programs: %s: %s", what, cudaGetErrorString(e));
+  };
+  cudaError_t e = cudaMemsetAsync(flags, 0, 8, c.stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(bins, 0, 2 * nbin * sizeof(int), c.stream);
+  if (e != cudaSuccess) return fail(e, "memset");
   k_prog_sizes<<<grid, 256, 0, c.stream>>>(n, c.sch.items2, c.sch.order, c.nz, c.nc, (const float4 *)c.rec32,
-                                           (const int4 *)c.conn32, offs, flags, flags + 1);
+                                           (const int4 *)c.conn32, c.sch.stageOffset, nS, offs, bins, flags,
+                                           flags + 1);
   k_scan_local<<<(unsigned)nb, SCAN_NT, 0, c.stream>>>(n, offs, bsum);
   k_scan_totals<<<1, SCAN_NT, 0, c.stream>>>(nb, bsum);
   k_scan_add<<<grid, 256, 0, c.stream>>>(n, offs, bsum, flags);
-  unsigned long long total = 0;
-  unsigned hf[2] = {0, 0};
-  UMT_CUDA(cudaMemcpyAsync(&total, bsum + nb, 8, cudaMemcpyDeviceToHost, c.stream));
-  UMT_CUDA(cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c.stream));
-  UMT_CUDA(cudaStreamSynchronize(c.stream));
-  UMT_CUDA(cudaGetLastError());
+  e = cudaMemcpyAsync(&total, bsum + nb, 8, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hb.data(), bins, nbin * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(e, "size pass");
   if (hf[0] != 0 || hf[1] > (unsigned)P32_MAXCHUNK || total == 0) { cleanup(); return 0; }
+  // bin starts: stage offset + items of the stage's earlier bins
+  for (int s = 0; s < nS; ++s) {
+    int acc = c.sch.hOffset[s];
+    for (int b = 0; b < PROG_BINS; ++b) {
+      const int k = hb[(size_t)s * PROG_BINS + b];
+      hb[(size_t)s * PROG_BINS + b] = acc;
+      acc += k;
+    }
+    if (acc != c.sch.hOffset[s] + c.sch.hCount[s]) { cleanup(); return 0; }
+  }
   if (cudaMalloc((void **)&c.prog32, (size_t)total * 16) != cudaSuccess ||
       cudaMalloc((void **)&c.hdr32, (size_t)n * 16) != cudaSuccess) {
     if (c.prog32) cudaFree(c.prog32);
@@ -539,12 +625,16 @@ int prepare_prog32(Ctx &c) {
     cudaGetLastError();
     return 0;
   }
+  e = cudaMemcpyAsync(bins, hb.data(), nbin * sizeof(int), cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(bins + nbin, 0, nbin * sizeof(int), c.stream);
+  if (e != cudaSuccess) return fail(e, "bins");
   k_prog_write<<<grid, 256, 0, c.stream>>>(n, c.sch.items2, c.sch.order, c.nz, c.nc, (const float4 *)c.rec32,
-                                           (const int4 *)c.conn32, offs, (uint4 *)c.prog32, (uint4 *)c.hdr32,
-                                           flags);
-  UMT_CUDA(cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c.stream));
-  UMT_CUDA(cudaStreamSynchronize(c.stream));
-  UMT_CUDA(cudaGetLastError());
+                                           (const int4 *)c.conn32, c.sch.stageOffset, nS, offs, bins, bins + nbin,
+                                           (uint4 *)c.prog32, (uint4 *)c.hdr32, flags);
+  e = cudaMemcpyAsync(hf, flags, 8, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(e, "write pass");
   cleanup();
   if (hf[0] != 0) {
     cudaFree(c.prog32); cudaFree(c.hdr32);
@@ -570,7 +660,7 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   ProgP p;
   p.nz = c.nz; p.nc = c.nc; p.nb = c.nb;
   p.tstride = team_stride_p(c.G);
-  p.bstride = c.progMaxChunks * 16;
+  p.bstride = blob_stride_p(c.progMaxChunks);
   p.hdr = (const uint4 *)c.hdr32; p.prog = (const uint4 *)c.prog32;
   p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
   p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
