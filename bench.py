@@ -49,6 +49,14 @@ def b_alg(G: int, A: int, s_psi: int, s_g: int, ncf: int = 3) -> float:
     return 2 * s_psi + (s_g * 6 * ncf + 4 * 2 * ncf + s_g) / G + 16.0 / A
 
 
+# DRAM bytes (read + write) per corner*angle*group unit of the FP32 stage
+# kernels, summed over every stage launch of one whole sweep by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, 12^3 tiles, 128 directions,
+# 16 groups; the ncu summary is kept under profiles/).  Cold-cache per launch
+# under ncu; scaled by the units of the measured sweep.
+TRAFFIC_B_PER_UNIT_FP32_G16 = 13.876
+
+
 def peaks():
     try:
         d = json.load(open(MEASURED))
@@ -72,7 +80,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except Exception:
@@ -307,6 +315,7 @@ def main():
     k_avg = sum(kern_ms) / len(kern_ms)
     peak, src = peaks()
     achieved = balg * units / (k_avg * 1e-3) / 1e9
+    traffic = TRAFFIC_B_PER_UNIT_FP32_G16 * units if (s == 4 and G == 16) else None
     line = {
         "metric": METRIC, "value": value, "unit": "ns", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": False, "scaling": "weak",
@@ -318,8 +327,9 @@ def main():
                    "l2": "inputs larger than L2 (angular flux %.1f GB)" % (A * m.ncornr * G * s / 1e9),
                    "psi": "fp32" if s == 4 else "fp64", "tallies": "fp64"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": src,
-                     "kernel": "k_sweep (all dependency stages of one sweep)",
+                     "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per sweep",
+                     "peak_source": src,
+                     "kernel": "k_sweep32p (all dependency stages of one sweep)",
                      "bytes_per_unit": balg, "kernel_ms": k_avg, "tally_ms": sum(tally_ms) / len(tally_ms)},
         "e2e": {"value": t_e2e * 1e9 / (units * world), "unit": "ns", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
