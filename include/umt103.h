@@ -180,7 +180,8 @@ typedef struct UmtEnergyTally {
   double PowerEscape;       /* sum w (A_bdy.Omega>0) A_bdy.Omega psi         */
   double PowerIncident;     /* sum w (A_bdy.Omega<0) |A_bdy.Omega| psiB      */
   double PowerAbsorbed;     /* sum V sigma_a PhiTotal                        */
-  double Balance;           /* sweep balance residual (see DESIGN)          */
+  double Balance;           /* reserved; always 0 (the host forms the balance
+                               from the other four, as rtedit does)          */
 } UmtEnergyTally;
 
 int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *tally);

@@ -264,10 +264,7 @@ def build_tiled_mesh(nx: int, ny: int, nz: int) -> Mesh:
         (zoneOpp[zc[:, None].repeat(MAXCF, 1), CToFace] >= 0)[np.arange(MAXCF)[None, :] < nCFaces[:, None]]] >= 0).all()
 
     # ---- boundary elements: zone order, face order, corner order on face ----
-    bdy_c = []
-    for z_is_bdy in [None]:
-        pass
-    # vectorised: for each zone face on the boundary, its corners in face order
+    # for each zone face on the boundary, its corners in face order
     rows = []
     for p, t in enumerate(tmpl):
         zs = np.arange(p, nzones, nP)
@@ -286,7 +283,6 @@ def build_tiled_mesh(nx: int, ny: int, nz: int) -> Mesh:
     bdyToC = rows[:, 3].astype(np.int32)
     # corner face (c, i) on a boundary face -> ncornr + b
     key_b = (rows[:, 3] * MAXFACES + rows[:, 1])
-    lookup = dict()
     srt = np.argsort(key_b)
     key_sorted = key_b[srt]
     for i in range(MAXCF):

@@ -89,7 +89,8 @@ class Problem:
 
 
 def uniform_problem(tiles=(10, 10, 10), npolar=2, nazimuthal=2, ngr=2, dt=1.0e-3) -> Problem:
-    """The reference driver's built-in uniform material (BASELINE configuration 1)."""
+    """The reference driver's built-in uniform material (test_driver.cc:1163-1286):
+    sigma_a = 10 in every group, no scattering, Tr = 0.05 Planck initial intensity."""
     m = build_tiled_mesh(*tiles)
     omega, weight = product_quadrature(npolar, nazimuthal, 1)
     siga = np.full((m.nzones, ngr), 10.0)
@@ -105,7 +106,8 @@ def uniform_problem(tiles=(10, 10, 10), npolar=2, nazimuthal=2, ngr=2, dt=1.0e-3
 def synthetic_problem(tiles, npolar, nazimuthal, ngr, seed, sigt_range=(1e-2, 1e2),
                       c_range=(0.0, 0.5), q=1.0, n_materials=None, dt=1.0e-3,
                       time_dependent=False) -> Problem:
-    """Seeded multigroup problem with scattering (BASELINE configurations 2-5).
+    """Seeded multigroup problem with scattering (the scattering workloads: 20^3
+    and 30^3 tiles with 128 directions and 16 groups, batches of small problems).
 
     Opacities are drawn per zone (or per material, with a per-tile material
     index when n_materials is given) and per group; sigma_s = c*sigma_t and
