@@ -329,7 +329,8 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_unit": "bytes per sweep",
                      "peak_source": src,
-                     "kernel": "k_sweep32p (all dependency stages of one sweep)",
+                     "kernel": ("k_sweep32p" if s == 4 else "k_sweep<double>") +
+                               " (all dependency stages of one sweep)",
                      "bytes_per_unit": balg, "kernel_ms": k_avg, "tally_ms": sum(tally_ms) / len(tally_ms)},
         "e2e": {"value": t_e2e * 1e9 / (units * world), "unit": "ns", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
