@@ -174,9 +174,14 @@ class Library:
         check(self.lib.umt103_get_psi(_d(Psi), _d(PsiB), int(precision)))
         return Psi, PsiB
 
-    def sweep(self, STotal=None, savePsi=False, PsiB=None, precision=UMT_FP64, want_phi=True):
+    def sweep(self, STotal=None, savePsi=False, PsiB=None, precision=UMT_FP64, want_phi=True, Phi=None):
+        """umt103_sweep; Phi, if given, is a C-contiguous float64 (nc, G)
+        array the result is written into (e.g. a view of pinned memory)."""
         STotal = _c(STotal, np.float64)
-        Phi = np.zeros((self.nc, self.G)) if want_phi else None
+        if Phi is not None:
+            assert Phi.dtype == np.float64 and Phi.flags.c_contiguous and Phi.shape == (self.nc, self.G)
+        elif want_phi:
+            Phi = np.zeros((self.nc, self.G))
         if PsiB is not None:
             assert PsiB.dtype == np.float64 and PsiB.flags.c_contiguous
         check(self.lib.umt103_sweep(_d(STotal), int(bool(savePsi)), _d(Phi), _d(PsiB), int(precision)))

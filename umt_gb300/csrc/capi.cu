@@ -73,7 +73,8 @@ static void free_ctx(Ctx &c) {
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red);
   dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
-  dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch);
+  dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64);
+  c.stage64N = 0;
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
   if (c.evMid) cudaEventDestroy(c.evMid);
@@ -490,6 +491,20 @@ int umt103_get_phi(double *PhiTotal) {
   return 0;
 }
 
+// FP64 staging buffer for the FP32 path's PsiB conversions, allocated on the
+// first call that needs it and kept with the context (a per-call
+// allocation and free would synchronise the device every sweep).
+static int staging64(Ctx &c, size_t n, double **out) {
+  if (c.stage64N < n) {
+    dfree(c.stage64);
+    c.stage64N = 0;
+    TRY(dalloc(&c.stage64, n));
+    c.stage64N = n;
+  }
+  *out = c.stage64;
+  return 0;
+}
+
 int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double *PsiB_inout, int precision) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
@@ -501,27 +516,24 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
       UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
     } else {
       double *tmp = nullptr;
-      TRY(dalloc(&tmp, psiBN));
+      TRY(staging64(c, psiBN, &tmp));
       UMT_CUDA(cudaMemcpyAsync(tmp, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
       k_d2f<<<4096, 256, 0, c.stream>>>(psiBN, tmp, c.psiB32);
-      UMT_CUDA(cudaStreamSynchronize(c.stream));
-      cudaFree(tmp);
     }
   }
   TRY(sweep_core(savePsi, precision));
-  if (PhiTotal_out) UMT_CUDA(cudaMemcpy(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost));
+  if (PhiTotal_out) UMT_CUDA(cudaMemcpyAsync(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));
   if (PsiB_inout) {
     if (precision == UMT_FP64) {
-      UMT_CUDA(cudaMemcpy(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost));
+      UMT_CUDA(cudaMemcpyAsync(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
     } else {
       double *tmp = nullptr;
-      TRY(dalloc(&tmp, psiBN));
+      TRY(staging64(c, psiBN, &tmp));
       k_f2d<<<4096, 256, 0, c.stream>>>(psiBN, c.psiB32, tmp);
       UMT_CUDA(cudaMemcpyAsync(PsiB_inout, tmp, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
-      UMT_CUDA(cudaStreamSynchronize(c.stream));
-      cudaFree(tmp);
     }
   }
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
   return 0;
 }
 

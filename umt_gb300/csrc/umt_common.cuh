@@ -95,6 +95,8 @@ struct Ctx {
   unsigned int *status = nullptr;               // device status word
   double *scratch = nullptr;                    // reductions
   size_t scratchBytes = 0;
+  double *stage64 = nullptr;                    // FP64 staging of PsiB for FP32 sweeps (kept)
+  size_t stage64N = 0;
   // captured sweep graphs per precision
   cudaGraphExec_t graphs[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [precision][cur]
   bool useGraphs = true;
