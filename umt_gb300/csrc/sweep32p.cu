@@ -84,7 +84,7 @@ __device__ __forceinline__ float2 div2(float2 a, float2 b) {
 __host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 * 32; }
 
 template <int GT, int GPL>
-__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, int stage) {
+__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, int stage) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
   constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
   constexpr int G = GT * GPL;
@@ -120,10 +120,12 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
     for (int e = lane; e < nch; e += GT) cp_async16_cg(sB + 16 * e, src + e);
     const float *po = p.psi_old + (abase + c0) * G + g0;
     const float *st = p.STotal + (size_t)c0 * G + g0;
-    for (int c = 0; c < nC; ++c) {
-      cp_async(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4);
-      cp_async(sS + c * RP + g0, st + (size_t)c * G, GPL * 4);
-    }
+#pragma unroll
+    for (int c = 0; c < UMT_MAXCORNER; ++c)
+      if (c < nC) {
+        cp_async(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4);
+        cp_async(sS + c * RP + g0, st + (size_t)c * G, GPL * 4);
+      }
   }
   float2 sg[NP];
   ldg2<NP>(p.Sigt + (size_t)z * G + g0, sg);
@@ -141,38 +143,41 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 8 : 6) k_sweep32p(ProgP p, 
   const uint32_t *ex = reinterpret_cast<const uint32_t *>(pul + nD);
   // ---- corner sources: Q = tau*psi_old + STotal, S = V*Q ----
   const float2 tau2 = f2(p.tau);
-  for (int c = 0; c < nC; ++c) {
-    float2 q[NP], s[NP];
-    ld2<NP>(sQ + c * RP + g0, q);
-    ld2<NP>(sS + c * RP + g0, s);
-    const float2 v2 = f2(crec[c].y);
 #pragma unroll
-    for (int j = 0; j < NP; ++j) {
-      q[j] = __ffma2_rn(tau2, q[j], s[j]);
-      s[j] = __fmul2_rn(v2, q[j]);
+  for (int c = 0; c < UMT_MAXCORNER; ++c)
+    if (c < nC) {
+      float2 q[NP], s[NP];
+      ld2<NP>(sQ + c * RP + g0, q);
+      ld2<NP>(sS + c * RP + g0, s);
+      const float2 v2 = f2(crec[c].y);
+#pragma unroll
+      for (int j = 0; j < NP; ++j) {
+        q[j] = __ffma2_rn(tau2, q[j], s[j]);
+        s[j] = __fmul2_rn(v2, q[j]);
+      }
+      st2<NP>(sQ + c * RP + g0, q);
+      st2<NP>(sS + c * RP + g0, s);
     }
-    st2<NP>(sQ + c * RP + g0, q);
-    st2<NP>(sS + c * RP + g0, s);
-  }
   // ---- round trip 3: upwind fluxes; FP inflow and the EZ closure that uses them ----
   const int nF = nA + nB;
   for (int base = 0; base < nF; base += NFC) {
     float2 pf[NFC][NP];
+    uint32_t cd[NFC];
 #pragma unroll
     for (int j = 0; j < NFC; ++j) {
+      cd[j] = 0u;
       if (base + j < nF) {
-        const uint32_t code = fin[base + j].x;
-        const size_t idx = code & 0x0fffffffu;
-        ldg2<NP>(((code >> 31) ? psiBA : psiNew) + idx * G, pf[j]);
+        cd[j] = fin[base + j].x;
+        const size_t idx = cd[j] & 0x0fffffffu;
+        ldg2<NP>(((cd[j] >> 31) ? psiBA : psiNew) + idx * G, pf[j]);
       }
     }
 #pragma unroll
     for (int j = 0; j < NFC; ++j) {
       const int i = base + j;
       if (i < nF) {
-        const uint2 e = fin[i];
-        const int c = (e.x >> 28) & 7;
-        const float2 w2 = f2(__uint_as_float(e.y));
+        const int c = (cd[j] >> 28) & 7;
+        const float2 w2 = f2(__uint_as_float(fin[i].y));
         float2 sc[NP];
         ld2<NP>(sS + c * RP + g0, sc);
 #pragma unroll
