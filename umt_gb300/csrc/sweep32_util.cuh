@@ -33,6 +33,15 @@ __device__ __forceinline__ void cp_async_wait_all() {
 
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
+// Programmatic dependent launch: allow the next kernel of the stream to start
+// launching its blocks, and (in that next kernel) wait until the previous
+// kernel has completed and its memory writes are visible.  Without a
+// programmatic dependency the wait returns at once.
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <int NP>
 __device__ __forceinline__ void ld2(const float *p, float2 (&v)[NP]) {
   if constexpr (NP == 2) {

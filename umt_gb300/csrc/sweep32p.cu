@@ -90,6 +90,9 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   constexpr int G = GT * GPL;
   extern __shared__ float4 smem4[];
   const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  // The next stage's launch may start now: its blocks fill SMs as this
+  // stage's finish and run their independent first two round trips.
+  pdl_launch_dependents();
   const int k = blockIdx.x * TEAMS + team;
   if (k >= p.stageCount[stage]) return;            // whole teams leave together
   const unsigned tm = team_mask(GT, tid);
@@ -159,6 +162,10 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
       st2<NP>(sS + c * RP + g0, s);
     }
   // ---- round trip 3: upwind fluxes; FP inflow and the EZ closure that uses them ----
+  // Upwind fluxes were written by earlier stages: wait for the previous
+  // stage's launch to complete (everything above reads only data that no
+  // stage of this sweep writes).
+  pdl_wait();
   const int nF = nA + nB;
   for (int base = 0; base < nF; base += NFC) {
     float2 pf[NFC][NP];
@@ -672,13 +679,23 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
   const int TEAMS = P32_NT / GT;
   const size_t smem = (size_t)TEAMS * ((size_t)p.tstride * 4 + p.bstride);
+  // Stage 0 follows the source conversion with ordinary stream order; every
+  // later stage is launched as a programmatic dependent of the one before.
+  cudaLaunchAttribute pdl[1];
+  pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  pdl[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(P32_NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = c.stream;
 #define UMT_LAUNCHP(gt, gpl)                                                                   \
   if (GT == gt && GPL == gpl) {                                                                \
     for (int s = 0; s < c.sch.nStages; ++s) {                                                  \
-      const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                \
-      k_sweep32p<gt, gpl><<<blocks, P32_NT, smem, c.stream>>>(p, s);                           \
+      cfg.gridDim = dim3((c.sch.hCount[s] + TEAMS - 1) / TEAMS);                               \
+      cfg.attrs = s > 0 && c.usePDL ? pdl : nullptr;                                           \
+      cfg.numAttrs = s > 0 && c.usePDL ? 1 : 0;                                                \
+      UMT_CUDA(cudaLaunchKernelEx(&cfg, k_sweep32p<gt, gpl>, p, s));                           \
     }                                                                                          \
-    UMT_CUDA(cudaGetLastError());                                                              \
     return 0;                                                                                  \
   }
   UMT_LAUNCHP(1, 2) UMT_LAUNCHP(2, 2) UMT_LAUNCHP(4, 2) UMT_LAUNCHP(8, 2) UMT_LAUNCHP(16, 2) UMT_LAUNCHP(32, 2)

@@ -73,6 +73,7 @@ struct Ctx {
   size_t progBytes = 0;
   int progMaxChunks = 0;                        // longest program, 16-byte units
   int progState = 0;                            // 0 not built, 1 built, -1 unavailable
+  bool usePDL = true;                           // stage launches as programmatic dependents
   int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
   int *ticket = nullptr;                        // persistent-mode work ticket
   Schedule sch;
