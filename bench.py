@@ -51,10 +51,10 @@ def b_alg(G: int, A: int, s_psi: int, s_g: int, ncf: int = 3) -> float:
 
 # DRAM bytes (read + write) per corner*angle*group unit of the FP32 stage
 # kernels, summed over every stage launch of one whole sweep by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum, 12^3 tiles, 128 directions,
-# 16 groups; the ncu summary is kept under profiles/).  Cold-cache per launch
-# under ncu; scaled by the units of the measured sweep.
-TRAFFIC_B_PER_UNIT_FP32_G16 = 13.876
+# (dram__bytes_read.sum + dram__bytes_write.sum with --cache-control none,
+# 12^3 tiles, 128 directions, 16 groups; the ncu summary is kept under
+# profiles/); scaled by the units of the measured sweep.
+TRAFFIC_B_PER_UNIT_FP32_G16 = 14.166
 
 
 def peaks():
