@@ -156,3 +156,33 @@ def test_batch_of_contexts_matches_single_runs(umtlib):
     umtlib.context_select(0)
     for cid in ids:
         umtlib.context_destroy(cid)
+
+
+def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):
+    """Page-locked and pageable host arrays give bit-identical sweeps, with
+    incoming boundary fluxes set and exits returned (the bench passes
+    page-locked buffers)."""
+    torch = pytest.importorskip("torch")
+    prob = synthetic_problem((3, 2, 2), 2, 2, 8, seed=9, time_dependent=True)
+    m = prob.mesh
+    A, G = len(prob.weight), prob.ngr
+    rng = np.random.default_rng(3)
+    PsiB0 = rng.uniform(0.0, 0.1, size=(A, m.nbelem, G))
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    out = []
+    for pinned in (False, True):
+        umtlib.init(m, prob.omega, prob.weight, G, flags=2 | 8)
+        umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+        umtlib.set_psi(prob.psi0, None)
+        if pinned:
+            PsiB = torch.empty((A, m.nbelem, G), dtype=torch.float64, pin_memory=True).numpy()
+            Phi = torch.empty((m.ncornr, G), dtype=torch.float64, pin_memory=True).numpy()
+        else:
+            PsiB = np.empty((A, m.nbelem, G))
+            Phi = np.empty((m.ncornr, G))
+        PsiB[...] = PsiB0
+        umtlib.sweep(STotal, savePsi=True, PsiB=PsiB, precision=capi.UMT_FP32, Phi=Phi)
+        out.append((Phi.copy(), PsiB.copy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert not np.array_equal(out[1][1], PsiB0)                   # exits were written back

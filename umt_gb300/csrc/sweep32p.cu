@@ -47,6 +47,8 @@ constexpr int P32_MAXCHUNK = 48;        // 16-byte units: 8 + 8*(8+24+24+24) + 4
 
 struct ProgP {
   int nz, nc, nb, tstride, bstride;     // tstride: floats per team (Q and S arrays); bstride: program bytes per team
+  uint32_t nzMagic;                     // a = (it * nzMagic) >> nzShift equals it / nz for it < 2^31
+  int nzShift;
   const uint4 *hdr;
   const int *stageOffset, *stageCount;
   const uint4 *prog;
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   const uint4 h = p.hdr[p.stageOffset[stage] + k];
   const bool bad = (h.x >> 31) != 0;
   const uint32_t it = h.x & 0x7fffffffu;
-  const int a = (int)(it / (uint32_t)p.nz);
+  const int a = (int)(((unsigned long long)it * p.nzMagic) >> p.nzShift);
   const int z = (int)(it - (uint32_t)a * p.nz);
   const int c0 = (int)(h.y & 0x0fffffffu), nC = (int)(h.y >> 28);
   const uint32_t ord = h.w & 0xffffffu;
@@ -671,6 +673,15 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   if (c.progState != 1 || !sweep32p_supported(c.G, GT, GPL)) return 1;
   ProgP p;
   p.nz = c.nz; p.nc = c.nc; p.nb = c.nb;
+  {
+    // division by the invariant nz as a multiply-high (round-up method):
+    // s = ceil(log2 nz), m = ceil(2^(31+s) / nz) < 2^32; exact for it < 2^31
+    int s = 0;
+    while ((1ll << s) < (long long)c.nz) ++s;
+    const unsigned long long m = ((1ull << (31 + s)) + (unsigned long long)c.nz - 1) / (unsigned long long)c.nz;
+    p.nzMagic = (uint32_t)m;
+    p.nzShift = 31 + s;
+  }
   p.tstride = team_stride_p(c.G);
   p.bstride = blob_stride_p(c.progMaxChunks);
   p.hdr = (const uint4 *)c.hdr32; p.prog = (const uint4 *)c.prog32;
