@@ -15,6 +15,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libumt103.so")
 
 UMT_FP64, UMT_FP32 = 0, 1
+(UMT_OK, UMT_ERR_ARG, UMT_ERR_STATE, UMT_ERR_CUDA, UMT_ERR_CYCLE, UMT_ERR_TIMEOUT, UMT_ERR_BOUNDS,
+ UMT_ERR_NOMEM, UMT_ERR_NOTCONV) = (0, -1, -2, -3, -4, -5, -6, -7, -8)
 
 ERRORS = {0: "UMT_OK", -1: "UMT_ERR_ARG", -2: "UMT_ERR_STATE", -3: "UMT_ERR_CUDA",
           -4: "UMT_ERR_CYCLE", -5: "UMT_ERR_TIMEOUT", -6: "UMT_ERR_BOUNDS",

@@ -428,6 +428,7 @@ int umt103_get_psi(double *Psi, double *PsiB, int precision) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   const size_t psiN = (size_t)c.A * c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
   if (precision == UMT_FP64) {
     if (!c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
     if (Psi) UMT_CUDA(cudaMemcpy(Psi, c.psi64[c.cur64], psiN * 8, cudaMemcpyDeviceToHost));
@@ -456,6 +457,7 @@ int umt103_set_source(const double *STotal) {
 
 static int sweep_core(int savePsi, int precision) {
   Ctx &c = cur();
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
@@ -487,6 +489,7 @@ int umt103_sweep_resident(int savePsi, int precision) {
 int umt103_get_phi(double *PhiTotal) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!PhiTotal) return set_error(UMT_ERR_ARG, "null PhiTotal");
   UMT_CUDA(cudaMemcpy(PhiTotal, c.Phi, (size_t)c.nc * c.G * 8, cudaMemcpyDeviceToHost));
   return 0;
 }
@@ -508,6 +511,9 @@ static int staging64(Ctx &c, size_t n, double **out) {
 int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double *PsiB_inout, int precision) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
+  if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
+  if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
   else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
@@ -742,6 +748,7 @@ int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *t) {
 int umt103_tally_precision(const double *siga, double speed_light, int precision, UmtEnergyTally *t) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   if (!t || !(speed_light > 0.0)) return set_error(UMT_ERR_ARG, "bad tally arguments");
