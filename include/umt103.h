@@ -220,6 +220,54 @@ int umt103_tally_noalloc(const double *siga_dev, double speed_light, int precisi
 /* Schedule statistics for one direction. */
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);
 
+/* ---------------------------------------------------------------------------
+ * 2-D cylindrical (RZ) geometry: the UCB sweep of snac/SweepUCBrz.F90 with
+ * the angular-derivative (half-angle intensity PsiM) terms, FP64.
+ * ------------------------------------------------------------------------- */
+
+/* RZ mesh: polygonal zones in the (r, z) half-plane, two corner faces per
+ * corner, Teton's RZ conventions (rt/geometryUCBrz.F90:48-150): a zone's
+ * corners counter-clockwise; cEZ[2c] the previous and cEZ[2c+1] the next
+ * corner of the zone (zone-local); corner face 0 on the edge to the next
+ * vertex, face 1 on the edge from the previous one; cFP the corner at the
+ * same vertex across that edge, or ncornr + b for boundary element b. */
+typedef struct UmtMeshRZ {
+  int index_base;            /* 0 or 1 (Fortran)                              */
+  int nzones, ncornr, nbelem, maxFaces;
+  const int *numCorner, *cOffSet, *zoneFaces;   /* [nzones]                   */
+  const int *zoneOpp, *faceOpp;                 /* [nzones*maxFaces]          */
+  const int *cFP, *cEZ, *CToFace;               /* [ncornr*2]                 */
+  const int *bdyToC;                            /* [nbelem]                   */
+  const double *px;                             /* [ncornr*2] (r, z)          */
+} UmtMeshRZ;
+
+/* RZ quadrature in sweep order (levels of fixed xi, each a starting
+ * direction, the weighted directions, a finishing direction; rt/quadrz.F90)
+ * with the angular coefficients of mods/AngleSet_mod.F90:335-346. */
+typedef struct UmtQuadRZ {
+  int nangles;
+  const double *omega;                          /* [nangles*2] (mu, xi)       */
+  const double *weight;                         /* [nangles]                  */
+  const double *angDerivFac, *quadTauW1, *quadTauW2;   /* [nangles]           */
+  const int *starting, *finishing;              /* [nangles] 0/1              */
+} UmtQuadRZ;
+
+/* Replaces the current context with an RZ problem: geometry (A_fp, A_ez,
+ * Area, Volume, RadiusFP, RadiusEZ) and every direction's schedule are built
+ * here; the directions of a level are swept in order (each needs the previous
+ * one's PsiM), the levels concurrently. */
+int umt103_init_rz(const UmtMeshRZ *mesh, const UmtQuadRZ *quad, int ngr, int flags);
+
+/* One SetSweep of the RZ problem (snac/SetSweep.F90 with SweepUCBrz): same
+ * arguments as umt103_sweep, FP64.  Finishing directions receive PsiM, as in
+ * the reference.  umt103_set_materials / umt103_set_psi / umt103_get_psi
+ * apply to the RZ context as to a 3-D one. */
+int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double *PsiB_inout);
+
+/* Copy out the RZ geometry: Area, Volume [ncornr], RadiusFP, RadiusEZ
+ * [ncornr*2] (any pointer may be NULL). */
+int umt103_get_geometry_rz(double *Area, double *Volume, double *RadiusFP, double *RadiusEZ);
+
 /* Copy out the device-built schedule: level of each (angle, zone) [A][nzones]
  * and per-angle hyperplane counts. */
 int umt103_get_schedule(int *level, int *nHyperPlanes);

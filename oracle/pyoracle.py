@@ -17,7 +17,8 @@ def lib():
     global _lib
     if _lib is None:
         _lib = C.CDLL(_build.build())
-        for name in ("orc_geometry", "orc_schedule", "orc_sweep_angle", "orc_set_sweep"):
+        for name in ("orc_geometry", "orc_schedule", "orc_sweep_angle", "orc_set_sweep", "orc_geometry_rz",
+                     "orc_set_sweep_rz"):
             getattr(_lib, name).restype = C.c_int
         _lib.orc_planck_groups.restype = None
     return _lib
@@ -62,6 +63,9 @@ class Schedule:
 
 
 def schedule(m, A_fp, A_ez, omega):
+    """Per-direction schedules; the number of corner faces per corner is taken
+    from the mesh (3 for the 3-D meshes, 2 for RZ)."""
+    maxcf = int(m.cFP.shape[1])
     A = omega.shape[0]
     nz, nc = m.nzones, m.ncornr
     S = Schedule(nz, nc, A)
@@ -73,7 +77,7 @@ def schedule(m, A_fp, A_ez, omega):
         om = np.ascontiguousarray(omega[a], np.float64)
         nzr = np.ascontiguousarray(S.nextZ[a]); ncr = np.ascontiguousarray(S.nextC[a])
         zip_ = np.ascontiguousarray(S.zonesInPlane[a])
-        nh = lib().orc_schedule(nz, nc, 3, m.zoneOpp.shape[1], _i(m.numCorner), _i(m.cOffSet),
+        nh = lib().orc_schedule(nz, nc, maxcf, m.zoneOpp.shape[1], _i(m.numCorner), _i(m.cOffSet),
                                 _i(m.zoneFaces), _i(m.zoneOpp), _i(m.faceOpp), _i(m.nCFaces),
                                 _i(m.CToFace), _i(m.cEZ), _d(A_fp), _d(A_ez), _d(om),
                                 _i(nzr), _i(ncr), _i(zip_), _i(cl), _i(ncyc))
@@ -116,3 +120,40 @@ def planck_groups(T, k, Bnorm, gnu):
     B = np.zeros(len(gnu) - 1)
     lib().orc_planck_groups(C.c_double(T), C.c_double(k), C.c_double(Bnorm), len(B), _d(gnu), _d(B))
     return B
+
+
+def geometry_rz(m):
+    """orc_geometry_rz: A_fp, A_ez [nc,2,3] (third component 0), Area, Volume [nc],
+    RadiusFP, RadiusEZ [nc,2], A_bdy [nb,3]."""
+    nc = m.ncornr
+    A_fp = np.zeros((nc, 2, 3)); A_ez = np.zeros((nc, 2, 3))
+    area = np.zeros(nc); vol = np.zeros(nc); rfp = np.zeros((nc, 2)); rez = np.zeros((nc, 2))
+    px = np.ascontiguousarray(m.px, np.float64)
+    rc = lib().orc_geometry_rz(m.nzones, nc, _i(m.numCorner), _i(m.cOffSet), _i(m.cEZ), _i(m.cFP), _d(px),
+                               _d(A_fp), _d(A_ez), _d(area), _d(vol), _d(rfp), _d(rez))
+    assert rc == 0
+    A_bdy = np.zeros((m.nbelem, 3))
+    for cc in range(nc):
+        for f in range(2):
+            v = int(m.cFP[cc, f])
+            if v >= nc:
+                A_bdy[v - nc] = A_fp[cc, f]
+    return dict(A_fp=A_fp, A_ez=A_ez, Area=area, Volume=vol, RadiusFP=rfp, RadiusEZ=rez, A_bdy=A_bdy)
+
+
+def set_sweep_rz(m, geo, S, Sigt, STotal, tau, omega3, q, Psi, PsiB, savePsi=False):
+    """orc_set_sweep_rz over all directions; returns Phi.  Psi/PsiB updated in place."""
+    A, nc, G = Psi.shape
+    Phi = np.zeros((nc, G))
+    i32 = lambda x: np.ascontiguousarray(x, np.int32)
+    d64 = lambda x: np.ascontiguousarray(x, np.float64)
+    rc = lib().orc_set_sweep_rz(
+        m.nzones, nc, m.nbelem, G, A, _i(m.numCorner), _i(m.cOffSet), _i(m.cFP), _i(m.cEZ),
+        _d(geo["A_fp"]), _d(geo["A_ez"]), _d(geo["Area"]), _d(geo["Volume"]), _d(geo["RadiusFP"]),
+        _d(geo["RadiusEZ"]), _d(d64(Sigt)), _d(d64(STotal)), C.c_double(tau), _d(d64(omega3)),
+        _d(d64(q.weight)), _d(d64(q.angDerivFac)), _d(d64(q.quadTauW1)), _d(d64(q.quadTauW2)),
+        _i(i32(q.starting)), _i(i32(q.finishing)), _i(S.nHyperPlanes), _i(S.zonesInPlane), _i(S.nextZ),
+        _i(S.nextC), _d(geo["A_bdy"]), _i(m.bdyToC), _d(Phi), _d(PsiB), _d(Psi), int(savePsi))
+    if rc != 0:
+        raise RuntimeError(f"orc_set_sweep_rz failed: {rc}")
+    return Phi

@@ -668,4 +668,211 @@ void orc_planck_groups(double T, double k, double Bnorm, int ngr, const double *
   B[ngr - 1] = full * (1.0 - lo);
 }
 
+// ---------------------------------------------------------------------------
+// 2-D RZ geometry: rt/geometryUCBrz.F90:36-150 (zone centre = vertex average,
+// mods/Geometry_mod.F90 getZoneCenter).  Two corner faces per corner; cEZ is
+// zone-local, cFP global (>= nc for a boundary element).  Face vectors are
+// written as 3-vectors with a zero third component, so the 3-D schedule
+// routines above order the RZ sweep.  The reference's `c < cfp` test compares
+// a zone-local with a global 1-based index; it is kept as written.
+// ---------------------------------------------------------------------------
+int orc_geometry_rz(int nz, int nc, const int *numCorner, const int *cOffSet, const int *cEZ, const int *cFP,
+                    const double *px, double *A_fp, double *A_ez, double *Area, double *Volume,
+                    double *RadiusFP, double *RadiusEZ) {
+  std::fill(A_fp, A_fp + (size_t)nc * 2 * 3, 0.0);
+  std::fill(A_ez, A_ez + (size_t)nc * 2 * 3, 0.0);
+  auto AF = [&](int cc, int f, int d) -> double & { return A_fp[((size_t)cc * 2 + f) * 3 + d]; };
+  auto AE = [&](int cc, int f, int d) -> double & { return A_ez[((size_t)cc * 2 + f) * 3 + d]; };
+  for (int zone = 0; zone < nz; ++zone) {
+    const int nC = numCorner[zone], c0 = cOffSet[zone];
+    double rz = 0.0, zz = 0.0;
+    for (int c = 0; c < nC; ++c) { rz += px[2 * (c0 + c)]; zz += px[2 * (c0 + c) + 1]; }
+    rz /= (double)nC;
+    zz /= (double)nC;
+    for (int c = 0; c < nC; ++c) {
+      const int cc = c0 + c;
+      const int c1 = cEZ[2 * cc], c2 = cEZ[2 * cc + 1];
+      const int cfp1 = cFP[2 * cc], cfp2 = cFP[2 * cc + 1];
+      const double r = px[2 * cc], z = px[2 * cc + 1];
+      const double r1 = px[2 * (c0 + c1)], z1 = px[2 * (c0 + c1) + 1];
+      const double r2 = px[2 * (c0 + c2)], z2 = px[2 * (c0 + c2) + 1];
+      const double re1 = 0.5 * (r + r1), ze1 = 0.5 * (z + z1);
+      const double re2 = 0.5 * (r + r2), ze2 = 0.5 * (z + z2);
+      RadiusFP[2 * cc] = 0.5 * (r + re2);
+      RadiusFP[2 * cc + 1] = 0.5 * (r + re1);
+      RadiusEZ[2 * cc] = 0.5 * (rz + re1);
+      RadiusEZ[2 * cc + 1] = 0.5 * (rz + re2);
+      if (c < cfp1) {                        // (c+1) < (cfp1+1) in the 1-based original
+        AF(cc, 0, 0) = 0.5 * (z2 - z);
+        AF(cc, 0, 1) = 0.5 * (r - r2);
+        if (cfp1 < nc) { AF(cfp1, 1, 0) = -AF(cc, 0, 0); AF(cfp1, 1, 1) = -AF(cc, 0, 1); }
+      }
+      if (c < cfp2) {
+        AF(cc, 1, 0) = 0.5 * (z - z1);
+        AF(cc, 1, 1) = 0.5 * (r1 - r);
+        if (cfp2 < nc) { AF(cfp2, 0, 0) = -AF(cc, 1, 0); AF(cfp2, 0, 1) = -AF(cc, 1, 1); }
+      }
+      if (c < c1) {
+        AE(cc, 0, 0) = ze1 - zz;
+        AE(cc, 0, 1) = rz - re1;
+        AE(c0 + c1, 1, 0) = -AE(cc, 0, 0);
+        AE(c0 + c1, 1, 1) = -AE(cc, 0, 1);
+      }
+      if (c < c2) {
+        AE(cc, 1, 0) = zz - ze2;
+        AE(cc, 1, 1) = re2 - rz;
+        AE(c0 + c2, 0, 0) = -AE(cc, 1, 0);
+        AE(c0 + c2, 0, 1) = -AE(cc, 1, 1);
+      }
+      const double area1 = std::fabs((re2 - r) * (zz - z) - (ze2 - z) * (rz - r));
+      const double area2 = std::fabs((rz - r) * (ze1 - z) - (zz - z) * (re1 - r));
+      Area[cc] = 0.5 * (area1 + area2);
+      const double rbar1 = (r + re2 + rz) / 3.0, rbar2 = (r + re1 + rz) / 3.0;
+      Volume[cc] = 0.5 * (rbar1 * area1 + rbar2 * area2);
+    }
+  }
+  return 0;
+}
+
+// One RZ direction: snac/SweepUCBrz.F90:87-276.  Psi1 [(nc+nb)][G] carries
+// the previous direction's values; PsiM [nc][G] is the half-angle intensity.
+static void sweep_rz_angle(int nz, int nc, int nb, int G, const int *numCorner, const int *cOffSet, const int *cFP,
+                           const int *cEZ, const double *A_fp, const double *A_ez, const double *Area,
+                           const double *Volume, const double *RadiusFP, const double *RadiusEZ, const double *Sigt,
+                           const double *STotal, double tau, const double *om, double quadwt, double fac,
+                           double W1, double W2, bool starting, int nHyper, const int *zonesInPlane,
+                           const int *nextZ, const int *nextC, const double *psiA, double *Psi1, double *PsiM,
+                           double *Phi) {
+  const double fouralpha = 1.82;
+  int maxC = 1;
+  for (int z = 0; z < nz; ++z) maxC = std::max(maxC, numCorner[z]);
+  std::vector<double> Q((size_t)maxC * G), src((size_t)maxC * G), coefpsi(2 * maxC);
+  std::vector<double> sumArea(maxC);
+  std::vector<int> nxez(maxC), ez_exit(2 * maxC);
+  int ndoneZ = 0;
+  for (int h = 0; h < nHyper; ++h) {
+    const int nzones = zonesInPlane[h];
+    for (int ii = 0; ii < nzones; ++ii) {
+      const int zone0 = nextZ[ndoneZ + ii];
+      const int zone = zone0 < 0 ? -zone0 - 1 : zone0;
+      const int nC = numCorner[zone], c0 = cOffSet[zone];
+      for (int c = 0; c < nC; ++c) {
+        nxez[c] = 0;
+        for (int g = 0; g < G; ++g) {
+          const double source = STotal[(size_t)(c0 + c) * G + g] + tau * psiA[(size_t)(c0 + c) * G + g];
+          Q[(size_t)c * G + g] = source;
+          src[(size_t)c * G + g] = Volume[c0 + c] * source;
+        }
+        sumArea[c] = fac * Area[c0 + c];
+      }
+      for (int c = 0; c < nC; ++c) {
+        const int cc = c0 + c;
+        for (int cface = 0; cface < 2; ++cface) {
+          const double afp = dot3(om, A_fp + ((size_t)cc * 2 + cface) * 3);
+          const double aez = dot3(om, A_ez + ((size_t)cc * 2 + cface) * 3);
+          int cfp = -1;
+          if (afp < 0.0) {
+            cfp = cFP[2 * cc + cface];
+            const double R_afp = RadiusFP[2 * cc + cface] * afp;
+            sumArea[c] = sumArea[c] - R_afp;
+            for (int g = 0; g < G; ++g)
+              src[(size_t)c * G + g] = src[(size_t)c * G + g] - R_afp * Psi1[(size_t)cfp * G + g];
+          }
+          if (aez > 0.0) {
+            const double R = RadiusEZ[2 * cc + cface];
+            const int cez = cEZ[2 * cc + cface];
+            const double area = Area[cc];
+            ez_exit[2 * c + nxez[c]] = cez;
+            coefpsi[2 * c + nxez[c]] = R * aez;
+            nxez[c] += 1;
+            sumArea[cez] = sumArea[cez] + R * aez;
+            if (afp < 0.0) {
+              for (int g = 0; g < G; ++g) {
+                const double sig = Sigt[(size_t)zone * G + g];
+                const double sigA = sig * area, sigA2 = sigA * sigA;
+                const double gnum = aez * aez * (fouralpha * sigA2 + aez * (4.0 * sigA + 3.0 * aez));
+                const double gden = area * (4.0 * sigA * sigA2 + aez * (6.0 * sigA2 + 2.0 * aez * (2.0 * sigA + aez)));
+                const double Qc = Q[(size_t)c * G + g], Qz = Q[(size_t)cez * G + g];
+                const double sez = R * (area * gnum * (sig * Psi1[(size_t)cfp * G + g] - Qc) +
+                                        0.5 * aez * gden * (Qc - Qz)) / (gnum + gden * sig);
+                src[(size_t)c * G + g] = src[(size_t)c * G + g] + sez;
+                src[(size_t)cez * G + g] = src[(size_t)cez * G + g] - sez;
+              }
+            } else {
+              for (int g = 0; g < G; ++g) {
+                const double Qc = Q[(size_t)c * G + g], Qz = Q[(size_t)cez * G + g];
+                const double sez = 0.5 * R * aez * (Qc - Qz) / Sigt[(size_t)zone * G + g];
+                src[(size_t)c * G + g] = src[(size_t)c * G + g] + sez;
+                src[(size_t)cez * G + g] = src[(size_t)cez * G + g] - sez;
+              }
+            }
+          }
+        }
+      }
+      for (int i = 0; i < nC; ++i) {
+        const int c = nextC[c0 + i];
+        for (int g = 0; g < G; ++g)
+          Psi1[(size_t)(c0 + c) * G + g] =
+              (src[(size_t)c * G + g] + Area[c0 + c] * fac * PsiM[(size_t)(c0 + c) * G + g]) /
+              (sumArea[c] + Sigt[(size_t)zone * G + g] * Volume[c0 + c]);
+        for (int f = 0; f < nxez[c]; ++f) {
+          const int cez = ez_exit[2 * c + f];
+          for (int g = 0; g < G; ++g)
+            src[(size_t)cez * G + g] = src[(size_t)cez * G + g] + coefpsi[2 * c + f] * Psi1[(size_t)(c0 + c) * G + g];
+        }
+      }
+      for (int c = 0; c < nC; ++c)
+        for (int g = 0; g < G; ++g) {
+          const size_t e = (size_t)(c0 + c) * G + g;
+          if (starting) {
+            PsiM[e] = Psi1[e];
+          } else {
+            PsiM[e] = W1 * Psi1[e] - W2 * PsiM[e];
+            Phi[e] = Phi[e] + quadwt * Psi1[e];
+          }
+        }
+    }
+    ndoneZ += nzones;
+  }
+}
+
+// The RZ part of SetSweep (snac/SetSweep.F90:56-111): PsiM zeroed, the
+// directions swept in quadrature order (finishing directions are not swept;
+// they receive PsiM), Psi1 carried from direction to direction.  Schedules are
+// packed per direction as for orc_set_sweep.
+int orc_set_sweep_rz(int nz, int nc, int nb, int G, int A, const int *numCorner, const int *cOffSet,
+                     const int *cFP, const int *cEZ, const double *A_fp, const double *A_ez, const double *Area,
+                     const double *Volume, const double *RadiusFP, const double *RadiusEZ, const double *Sigt,
+                     const double *STotal, double tau, const double *omega, const double *weight,
+                     const double *angDerivFac, const double *quadTauW1, const double *quadTauW2,
+                     const int *starting, const int *finishing, const int *nHyperPlanes, const int *zonesInPlane,
+                     const int *nextZ, const int *nextC, const double *A_bdy, const int *bdyToC, double *Phi,
+                     double *PsiB, double *Psi, int savePsi) {
+  std::vector<double> Psi1((size_t)(nc + nb) * G, 0.0), PsiM((size_t)nc * G, 0.0);
+  std::fill(Phi, Phi + (size_t)nc * G, 0.0);
+  for (int a = 0; a < A; ++a) {
+    if (finishing[a]) continue;
+    for (int b = 0; b < nb; ++b)
+      for (int g = 0; g < G; ++g) Psi1[(size_t)(nc + b) * G + g] = PsiB[((size_t)a * nb + b) * G + g];
+    sweep_rz_angle(nz, nc, nb, G, numCorner, cOffSet, cFP, cEZ, A_fp, A_ez, Area, Volume, RadiusFP, RadiusEZ, Sigt,
+                   STotal, tau, omega + 3 * a, weight[a], angDerivFac[a], quadTauW1[a], quadTauW2[a],
+                   starting[a] != 0, nHyperPlanes[a], zonesInPlane + (size_t)a * nz, nextZ + (size_t)a * nz,
+                   nextC + (size_t)a * nc, Psi + (size_t)a * nc * G, Psi1.data(), PsiM.data(), Phi);
+    const bool nextFinishing = a + 1 < A && finishing[a + 1];
+    for (int b = 0; b < nb; ++b) {
+      if (!(dot3(omega + 3 * a, A_bdy + 3 * b) > 0.0)) continue;        // exit list (rt/findexit.F90:305-317)
+      const int c = bdyToC[b];
+      for (int g = 0; g < G; ++g) {
+        PsiB[((size_t)a * nb + b) * G + g] = Psi1[(size_t)c * G + g];
+        if (nextFinishing) PsiB[((size_t)(a + 1) * nb + b) * G + g] = PsiM[(size_t)c * G + g];
+      }
+    }
+    if (savePsi) {
+      std::copy(Psi1.begin(), Psi1.begin() + (size_t)nc * G, Psi + (size_t)a * nc * G);
+      if (nextFinishing) std::copy(PsiM.begin(), PsiM.end(), Psi + (size_t)(a + 1) * nc * G);
+    }
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -1,0 +1,94 @@
+"""2-D RZ sweep (snac/SweepUCBrz.F90 with SetSweep's RZ angle order) through
+the C-ABI against the CPU oracle's restatement."""
+import numpy as np
+import pytest
+
+from umt_gb300 import capi
+from umt_gb300.mesh_rz import build_rz_mesh
+from umt_gb300.quadrature_rz import product_quadrature_rz
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(nr, nzr, P, Az, G, seed, distort=0.15):
+    m = build_rz_mesh(nr, nzr, distort=distort, seed=seed)
+    q = product_quadrature_rz(P, Az)
+    rng = np.random.default_rng(seed)
+    sigt = rng.uniform(0.2, 20.0, size=(m.nzones, G))
+    STotal = rng.uniform(0.05, 1.0, size=(m.ncornr, G))
+    psi0 = rng.uniform(0.01, 0.2, size=(len(q.weight), m.ncornr, G))
+    PsiB = rng.uniform(0.0, 0.05, size=(len(q.weight), m.nbelem, G))
+    return m, q, sigt, STotal, psi0, PsiB
+
+
+def _oracle(m, q, sigt, STotal, psi0, PsiB, tau):
+    from oracle import pyoracle as po
+    geo = po.geometry_rz(m)
+    om3 = np.zeros((len(q.weight), 3)); om3[:, :2] = q.omega
+    S = po.schedule(m, geo["A_fp"], geo["A_ez"], om3)
+    assert S.numCycles.sum() == 0
+    Psi = psi0.copy(); PB = PsiB.copy()
+    Phi = po.set_sweep_rz(m, geo, S, sigt, STotal, tau, om3, q, Psi, PB, savePsi=True)
+    return geo, Phi, Psi, PB
+
+
+@pytest.mark.parametrize("nr,nzr,P,Az,G,index_base", [(4, 3, 2, 2, 4, 0), (6, 5, 4, 3, 8, 0), (3, 4, 1, 2, 1, 1)])
+def test_rz_sweep_matches_oracle(umtlib, nr, nzr, P, Az, G, index_base):
+    m, q, sigt, STotal, psi0, PsiB = _problem(nr, nzr, P, Az, G, seed=nr * 10 + G)
+    tau = 0.7
+    geo, Phi_ref, Psi_ref, PsiB_ref = _oracle(m, q, sigt, STotal, psi0, PsiB, tau)
+    umtlib.init_rz(m, q, G, index_base=index_base)
+    g = umtlib.geometry_rz()
+    for k in ("Area", "Volume", "RadiusFP", "RadiusEZ"):
+        assert np.array_equal(g[k], geo[k]), k
+    umtlib.set_materials(sigt, np.zeros_like(sigt), tau)
+    umtlib.set_psi(psi0, None)
+    PB = PsiB.copy()
+    Phi = umtlib.sweep_rz(STotal, savePsi=True, PsiB=PB)
+    Psi, _ = umtlib.get_psi(capi.UMT_FP64)
+    assert rel_err(Phi, Phi_ref) < 1e-12
+    assert rel_err(Psi, Psi_ref) < 1e-12
+    assert rel_err(PB, PsiB_ref) < 1e-12
+    # finishing directions carry the level's last half-angle intensity
+    fin = np.nonzero(q.finishing)[0]
+    assert np.abs(Psi[fin]).max() > 0
+
+
+def test_rz_repeated_sweeps_and_source_iteration(umtlib):
+    """Several sweeps in a row (savePsi on and off) stay equal to the oracle's."""
+    m, q, sigt, STotal, psi0, PsiB = _problem(5, 4, 2, 2, 4, seed=3)
+    tau = 0.3
+    from oracle import pyoracle as po
+    geo = po.geometry_rz(m)
+    om3 = np.zeros((len(q.weight), 3)); om3[:, :2] = q.omega
+    S = po.schedule(m, geo["A_fp"], geo["A_ez"], om3)
+    umtlib.init_rz(m, q, 4)
+    umtlib.set_materials(sigt, np.zeros_like(sigt), tau)
+    umtlib.set_psi(psi0, None)
+    Psi_o = psi0.copy()
+    for save in (False, True, True):
+        PB_o = PsiB.copy(); PB_d = PsiB.copy()
+        Phi_o = po.set_sweep_rz(m, geo, S, sigt, STotal, tau, om3, q, Psi_o, PB_o, savePsi=save)
+        Phi_d = umtlib.sweep_rz(STotal, savePsi=save, PsiB=PB_d)
+        assert rel_err(Phi_d, Phi_o) < 1e-12
+        assert rel_err(PB_d, PB_o) < 1e-12
+
+
+def test_rz_errors(umtlib):
+    m, q, sigt, STotal, psi0, PsiB = _problem(2, 2, 1, 1, 2, seed=1)
+    bad = product_quadrature_rz(1, 1)
+    bad.finishing = bad.finishing.copy(); bad.finishing[-1] = False       # last level never finishes
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.init_rz(m, bad, 2)
+    assert e.value.code == capi.UMT_ERR_ARG
+    umtlib.init(*_tiny3d())
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.sweep_rz(None)
+    assert e.value.code == capi.UMT_ERR_STATE
+
+
+def _tiny3d():
+    from umt_gb300.problems import uniform_problem
+    p = uniform_problem((1, 1, 1), 1, 1, 2)
+    return p.mesh, p.omega, p.weight, p.ngr

@@ -26,6 +26,7 @@ UNITS = {
     "sweep32.cu": [],
     "sweep32p.cu": [],
     "si.cu": [],
+    "rz.cu": ["-Xcompiler", "-ffp-contract=off"],   # host-side RZ geometry, same rounding as the Fortran
     "noalloc.cu": [],
 }
 

@@ -39,6 +39,18 @@ class UmtQuad(C.Structure):
     _fields_ = [("nangles", C.c_int), ("omega", _dp), ("weight", _dp)]
 
 
+class UmtMeshRZ(C.Structure):
+    _fields_ = [("index_base", C.c_int), ("nzones", C.c_int), ("ncornr", C.c_int), ("nbelem", C.c_int),
+                ("maxFaces", C.c_int), ("numCorner", _ip), ("cOffSet", _ip), ("zoneFaces", _ip),
+                ("zoneOpp", _ip), ("faceOpp", _ip), ("cFP", _ip), ("cEZ", _ip), ("CToFace", _ip),
+                ("bdyToC", _ip), ("px", _dp)]
+
+
+class UmtQuadRZ(C.Structure):
+    _fields_ = [("nangles", C.c_int), ("omega", _dp), ("weight", _dp), ("angDerivFac", _dp),
+                ("quadTauW1", _dp), ("quadTauW2", _dp), ("starting", _ip), ("finishing", _ip)]
+
+
 class UmtSIParams(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_iters", C.c_int), ("rel_tol", C.c_double),
                 ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int), ("warm_start", C.c_int)]
@@ -81,6 +93,7 @@ def load():
                   "umt103_last_timing", "umt103_launches_per_sweep", "umt103_select_device",
                   "umt103_set_group_tile", "umt103_tally_precision", "umt103_set_sweep_mode",
                   "umt103_set_gta", "umt103_tally_noalloc", "umt103_context_create",
+                  "umt103_init_rz", "umt103_sweep_rz", "umt103_get_geometry_rz",
                   "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
                   "umt103_batch_sweep"):
             getattr(_lib, n).restype = C.c_int
@@ -99,7 +112,8 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision",
             "umt103_set_sweep_mode", "umt103_set_gta", "umt103_tally_noalloc",
             "umt103_context_create", "umt103_context_select", "umt103_context_current",
-            "umt103_context_destroy", "umt103_batch_sweep"]
+            "umt103_context_destroy", "umt103_batch_sweep", "umt103_init_rz", "umt103_sweep_rz",
+            "umt103_get_geometry_rz"]
 
 
 def check(rc):
@@ -285,3 +299,45 @@ class Library:
         afp = np.zeros((self.nc, 3, 3)); aez = np.zeros((self.nc, 3, 3)); vol = np.zeros(self.nc)
         check(self.lib.umt103_get_geometry(_d(afp), _d(aez), _d(vol)))
         return afp, aez, vol
+
+    # ---- 2-D RZ geometry ----
+    def init_rz(self, mesh, quad, ngr, index_base=0):
+        """umt103_init_rz with a umt_gb300.mesh_rz.MeshRZ and a
+        umt_gb300.quadrature_rz.QuadRZ."""
+        m = mesh
+        a = dict(numCorner=_c(m.numCorner, np.int32), cOffSet=_c(m.cOffSet, np.int32),
+                 zoneFaces=_c(m.zoneFaces, np.int32), zoneOpp=_c(m.zoneOpp, np.int32),
+                 faceOpp=_c(m.faceOpp, np.int32), cFP=_c(m.cFP, np.int32), cEZ=_c(m.cEZ, np.int32),
+                 CToFace=_c(m.CToFace, np.int32), bdyToC=_c(m.bdyToC, np.int32))
+        if index_base == 1:
+            for k in ("cFP", "cEZ", "CToFace", "bdyToC"):      # cOffSet is an offset in both conventions
+                a[k] = a[k] + 1
+            zo = a["zoneOpp"].copy(); zo[zo >= 0] += 1; a["zoneOpp"] = zo
+            fo = a["faceOpp"].copy(); fo[fo >= 0] += 1; a["faceOpp"] = fo
+        px = _c(m.px, np.float64)
+        st = UmtMeshRZ(index_base, m.nzones, m.ncornr, m.nbelem, m.zoneOpp.shape[1], _i(a["numCorner"]),
+                       _i(a["cOffSet"]), _i(a["zoneFaces"]), _i(a["zoneOpp"]), _i(a["faceOpp"]), _i(a["cFP"]),
+                       _i(a["cEZ"]), _i(a["CToFace"]), _i(a["bdyToC"]), _d(px))
+        q = quad
+        arrs = [_c(q.omega, np.float64), _c(q.weight, np.float64), _c(q.angDerivFac, np.float64),
+                _c(q.quadTauW1, np.float64), _c(q.quadTauW2, np.float64), _c(q.starting, np.int32),
+                _c(q.finishing, np.int32)]
+        qs = UmtQuadRZ(len(q.weight), _d(arrs[0]), _d(arrs[1]), _d(arrs[2]), _d(arrs[3]), _d(arrs[4]),
+                       _i(arrs[5]), _i(arrs[6]))
+        self._keep = [a, px, arrs]
+        check(self.lib.umt103_init_rz(C.byref(st), C.byref(qs), int(ngr), 0))
+        self.A, self.G, self.nz, self.nc, self.nb = len(q.weight), int(ngr), m.nzones, m.ncornr, m.nbelem
+        return self
+
+    def sweep_rz(self, STotal=None, savePsi=False, PsiB=None):
+        STotal = _c(STotal, np.float64)
+        Phi = np.zeros((self.nc, self.G))
+        if PsiB is not None:
+            assert PsiB.dtype == np.float64 and PsiB.flags.c_contiguous
+        check(self.lib.umt103_sweep_rz(_d(STotal), int(bool(savePsi)), _d(Phi), _d(PsiB)))
+        return Phi
+
+    def geometry_rz(self):
+        area = np.zeros(self.nc); vol = np.zeros(self.nc); rfp = np.zeros((self.nc, 2)); rez = np.zeros((self.nc, 2))
+        check(self.lib.umt103_get_geometry_rz(_d(area), _d(vol), _d(rfp), _d(rez)))
+        return dict(Area=area, Volume=vol, RadiusFP=rfp, RadiusEZ=rez)

@@ -78,6 +78,7 @@ static void free_ctx(Ctx &c) {
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
   if (c.evMid) cudaEventDestroy(c.evMid);
+  free_rz(c);
   if (c.stream) cudaStreamDestroy(c.stream);
   c = Ctx();
 }
@@ -777,3 +778,15 @@ int umt103_tally_precision(const double *siga, double speed_light, int precision
 }
 
 }  // extern "C"
+
+namespace umt {
+
+// Context set-up and release for the other front ends of the library (the
+// RZ entry points in rz.cu): the same validation, uploads, projections and
+// device schedule as umt103_init, without the grey context.
+int init_context(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags) {
+  return init_ctx(c, m, q, ngr, flags);
+}
+void release_current_context() { free_all(); }
+
+}  // namespace umt

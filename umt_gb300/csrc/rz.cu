@@ -1,0 +1,445 @@
+// rz.cu -- the 2-D cylindrical (RZ) UCB sweep, FP64.
+//
+// Arithmetic of snac/SweepUCBrz.F90:87-276 (R-weighted face terms, the
+// angular-derivative term with the half-angle intensity PsiM) and the RZ part
+// of snac/SetSweep.F90: the directions of one xi-level are swept in
+// quadrature order, each starting from the PsiM the previous one left;
+// finishing directions are not swept and receive PsiM.
+//
+// The corner-face vectors are 2-vectors; they are stored as 3-vectors with a
+// zero third component, so the device schedule of the 3-D path (face-sign
+// dependencies, corner order, hyperplane levels) orders every RZ direction
+// unchanged.  Stages: the levels run concurrently, the directions of a level
+// back to back, so the item (direction a, zone z) of level L sits at stage
+// offset(a) + hyperplane(a, z), offset(a) being the hyperplanes of the
+// level's earlier swept directions.  One kernel launch per stage; a team of
+// GT lanes per item, lanes over groups, as in the FP64 kernel of sweep.cu.
+#include "umt_common.cuh"
+#include "../../include/umt103.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace umt {
+
+int init_context(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags);
+void release_current_context();
+
+struct RZData {
+  double *Area = nullptr, *RadiusFP = nullptr, *RadiusEZ = nullptr;   // [nc], [nc*2]
+  double *angDerivFac = nullptr, *W1 = nullptr, *W2 = nullptr;        // [A]
+  int *starting = nullptr, *nextFinishing = nullptr, *level = nullptr; // [A]
+  int *cFP2 = nullptr, *cEZ2 = nullptr;                              // [nc*2], 0-based
+  double *PsiM = nullptr;                                            // [nLevels][nc][G]
+  uint32_t *items = nullptr;                                         // stage order, a*nz + z
+  int nLevels = 0, nStages = 0, maxStageItems = 0;
+  std::vector<int> hCount, hOffset;
+  std::vector<double> hArea, hVolume, hRfp, hRez;
+};
+
+void free_rz(Ctx &c) {
+  RZData *r = c.rz;
+  if (!r) return;
+  for (void *p : {(void *)r->Area, (void *)r->RadiusFP, (void *)r->RadiusEZ, (void *)r->angDerivFac, (void *)r->W1,
+                  (void *)r->W2, (void *)r->starting, (void *)r->nextFinishing, (void *)r->level, (void *)r->cFP2,
+                  (void *)r->cEZ2, (void *)r->PsiM, (void *)r->items})
+    if (p) cudaFree(p);
+  delete r;
+  c.rz = nullptr;
+}
+
+template <typename T>
+static int upload(T **d, const T *h, size_t n) {
+  if (cudaMalloc((void **)d, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess)
+    return set_error(UMT_ERR_NOMEM, "RZ: device allocation of %zu bytes failed", n * sizeof(T));
+  if (n) UMT_CUDA(cudaMemcpy(*d, h, n * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// rt/geometryUCBrz.F90:48-150 per corner (zone centre = vertex average,
+// mods/Geometry_mod.F90 getZoneCenter).  Each corner's face vectors are
+// formed from its own vertices; the reference's writes of a neighbour's
+// entries give the same values (exact negations of the same differences).
+static void geometry_rz(int nz, const int *numCorner, const int *cOffSet, const int *cEZ, const double *px,
+                        std::vector<double> &A_fp, std::vector<double> &A_ez, RZData &r) {
+  const size_t nc = r.hArea.size();
+  A_fp.assign(nc * 2 * 3, 0.0);
+  A_ez.assign(nc * 2 * 3, 0.0);
+  for (int zone = 0; zone < nz; ++zone) {
+    const int nC = numCorner[zone], c0 = cOffSet[zone];
+    double rz = 0.0, zz = 0.0;
+    for (int c = 0; c < nC; ++c) { rz += px[2 * (c0 + c)]; zz += px[2 * (c0 + c) + 1]; }
+    rz /= (double)nC;
+    zz /= (double)nC;
+    for (int c = 0; c < nC; ++c) {
+      const size_t cc = (size_t)c0 + c;
+      const int c1 = cEZ[2 * cc], c2 = cEZ[2 * cc + 1];
+      const double r0 = px[2 * cc], z0 = px[2 * cc + 1];
+      const double r1 = px[2 * (c0 + c1)], z1 = px[2 * (c0 + c1) + 1];
+      const double r2 = px[2 * (c0 + c2)], z2 = px[2 * (c0 + c2) + 1];
+      const double re1 = 0.5 * (r0 + r1), ze1 = 0.5 * (z0 + z1);
+      const double re2 = 0.5 * (r0 + r2), ze2 = 0.5 * (z0 + z2);
+      r.hRfp[2 * cc] = 0.5 * (r0 + re2);
+      r.hRfp[2 * cc + 1] = 0.5 * (r0 + re1);
+      r.hRez[2 * cc] = 0.5 * (rz + re1);
+      r.hRez[2 * cc + 1] = 0.5 * (rz + re2);
+      A_fp[(cc * 2 + 0) * 3 + 0] = 0.5 * (z2 - z0);
+      A_fp[(cc * 2 + 0) * 3 + 1] = 0.5 * (r0 - r2);
+      A_fp[(cc * 2 + 1) * 3 + 0] = 0.5 * (z0 - z1);
+      A_fp[(cc * 2 + 1) * 3 + 1] = 0.5 * (r1 - r0);
+      A_ez[(cc * 2 + 0) * 3 + 0] = ze1 - zz;
+      A_ez[(cc * 2 + 0) * 3 + 1] = rz - re1;
+      A_ez[(cc * 2 + 1) * 3 + 0] = zz - ze2;
+      A_ez[(cc * 2 + 1) * 3 + 1] = re2 - rz;
+      const double area1 = std::fabs((re2 - r0) * (zz - z0) - (ze2 - z0) * (rz - r0));
+      const double area2 = std::fabs((rz - r0) * (ze1 - z0) - (zz - z0) * (re1 - r0));
+      r.hArea[cc] = 0.5 * (area1 + area2);
+      const double rbar1 = (r0 + re2 + rz) / 3.0, rbar2 = (r0 + re1 + rz) / 3.0;
+      r.hVolume[cc] = 0.5 * (rbar1 * area1 + rbar2 * area2);
+    }
+  }
+}
+
+struct RZP {
+  int nz, nc, nb, G;
+  const uint32_t *items;
+  int stageBegin, stageCount;
+  const uint32_t *order;
+  const int *numCorner, *cOffSet, *cFP2, *cEZ2;
+  const double *afp, *aez;               // [A][nc][UMT_MAXCF] projections
+  const double *Area, *Volume, *RadiusFP, *RadiusEZ;
+  const double *Sigt, *STotal;
+  double tau;
+  const double *angDerivFac, *W1, *W2;
+  const int *starting, *nextFinishing, *level;
+  const double *psi_old;
+  double *psi_new, *psiB, *PsiM;
+};
+
+constexpr int RZ_NT = 128;
+constexpr int RZ_MAXC = UMT_MAXCORNER;
+
+template <int GT>
+__global__ void __launch_bounds__(RZ_NT) k_sweep_rz(RZP p) {
+  constexpr int TEAMS = RZ_NT / GT;
+  __shared__ double s_src[RZ_MAXC][RZ_NT];
+  __shared__ double s_Q[RZ_MAXC][RZ_NT];
+  __shared__ double s_afp[TEAMS][RZ_MAXC][2], s_aez[TEAMS][RZ_MAXC][2];
+  __shared__ double s_rfp[TEAMS][RZ_MAXC][2], s_rez[TEAMS][RZ_MAXC][2];
+  __shared__ double s_area[TEAMS][RZ_MAXC], s_vol[TEAMS][RZ_MAXC], s_sum[TEAMS][RZ_MAXC];
+  __shared__ int s_cfp[TEAMS][RZ_MAXC][2];
+  __shared__ int8_t s_cez[TEAMS][RZ_MAXC][2];
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const int k = blockIdx.x * TEAMS + team;
+  if (k >= p.stageCount) return;                       // whole teams leave together
+  const unsigned teammask = (GT == 32) ? 0xffffffffu : (((1u << GT) - 1u) << ((tid & 31) / GT * GT));
+  const uint32_t it = p.items[p.stageBegin + k];
+  const int a = (int)(it / (uint32_t)p.nz);
+  const int z = (int)(it - (uint32_t)a * p.nz);
+  const int nC = p.numCorner[z], c0 = p.cOffSet[z];
+  const uint32_t ord = p.order[it];
+  const size_t abase = (size_t)a * p.nc;
+  const double fac = p.angDerivFac[a];
+  for (int c = lane; c < nC; c += GT) {
+    const size_t cc = (size_t)c0 + c;
+    s_area[team][c] = p.Area[cc];
+    s_vol[team][c] = p.Volume[cc];
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      s_afp[team][c][f] = p.afp[(abase + cc) * UMT_MAXCF + f];
+      s_aez[team][c][f] = p.aez[(abase + cc) * UMT_MAXCF + f];
+      s_rfp[team][c][f] = p.RadiusFP[2 * cc + f];
+      s_rez[team][c][f] = p.RadiusEZ[2 * cc + f];
+      s_cfp[team][c][f] = p.cFP2[2 * cc + f];
+      s_cez[team][c][f] = (int8_t)p.cEZ2[2 * cc + f];
+    }
+  }
+  __syncwarp(teammask);
+  // sumArea in the reference's order: fac*Area for every corner, then the
+  // corner / corner-face loop (SweepUCBrz.F90:128-151)
+  if (lane == 0) {
+    for (int c = 0; c < nC; ++c) s_sum[team][c] = fac * s_area[team][c];
+    for (int c = 0; c < nC; ++c)
+      for (int f = 0; f < 2; ++f) {
+        const double afp = s_afp[team][c][f], aez = s_aez[team][c][f];
+        if (afp < 0.0) s_sum[team][c] = s_sum[team][c] - s_rfp[team][c][f] * afp;
+        if (aez > 0.0) {
+          const int cez = s_cez[team][c][f];
+          s_sum[team][cez] = s_sum[team][cez] + s_rez[team][c][f] * aez;
+        }
+      }
+  }
+  __syncwarp(teammask);
+  const double fouralpha = 1.82;
+  const double *sigz = p.Sigt + (size_t)z * p.G;
+  const bool start = p.starting[a] != 0, nextFin = p.nextFinishing[a] != 0;
+  double *psiM = p.PsiM + (size_t)p.level[a] * p.nc * p.G;
+  for (int g = lane; g < p.G; g += GT) {
+    const double sig = sigz[g];
+    for (int c = 0; c < nC; ++c) {
+      const size_t e = ((size_t)c0 + c) * p.G + g;
+      const double q = p.STotal[e] + p.tau * p.psi_old[abase * p.G + e];
+      s_Q[c][tid] = q;
+      s_src[c][tid] = s_vol[team][c] * q;
+    }
+    for (int c = 0; c < nC; ++c) {
+      for (int f = 0; f < 2; ++f) {
+        const double afp = s_afp[team][c][f], aez = s_aez[team][c][f];
+        double pu = 0.0;
+        if (afp < 0.0) {
+          const int cfp = s_cfp[team][c][f];
+          pu = (cfp < p.nc) ? p.psi_new[(abase + cfp) * p.G + g]
+                            : p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g];
+          const double R_afp = s_rfp[team][c][f] * afp;
+          s_src[c][tid] = s_src[c][tid] - R_afp * pu;
+        }
+        if (aez > 0.0) {
+          const double R = s_rez[team][c][f];
+          const int cez = s_cez[team][c][f];
+          const double area = s_area[team][c];
+          const double Qc = s_Q[c][tid], Qz = s_Q[cez][tid];
+          double sez;
+          if (afp < 0.0) {
+            const double sigA = sig * area, sigA2 = sigA * sigA;
+            const double gnum = aez * aez * (fouralpha * sigA2 + aez * (4.0 * sigA + 3.0 * aez));
+            const double gden = area * (4.0 * sigA * sigA2 + aez * (6.0 * sigA2 + 2.0 * aez * (2.0 * sigA + aez)));
+            sez = R * (area * gnum * (sig * pu - Qc) + 0.5 * aez * gden * (Qc - Qz)) / (gnum + gden * sig);
+          } else {
+            sez = 0.5 * R * aez * (Qc - Qz) / sig;
+          }
+          s_src[c][tid] = s_src[c][tid] + sez;
+          s_src[cez][tid] = s_src[cez][tid] - sez;
+        }
+      }
+    }
+    double *out = p.psi_new + abase * p.G;
+    for (int i = 0; i < nC; ++i) {
+      const int c = (int)((ord >> (4 * i)) & 15u);
+      const size_t e = ((size_t)c0 + c) * p.G + g;
+      const double v = (s_src[c][tid] + s_area[team][c] * fac * psiM[e]) / (s_sum[team][c] + sig * s_vol[team][c]);
+      out[e] = v;
+      s_Q[c][tid] = v;                       // Q is no longer needed: keep the solved flux
+      for (int f = 0; f < 2; ++f) {
+        const double aez = s_aez[team][c][f];
+        if (aez > 0.0) {
+          const int cez = s_cez[team][c][f];
+          s_src[cez][tid] = s_src[cez][tid] + (s_rez[team][c][f] * aez) * v;
+        }
+      }
+    }
+    for (int c = 0; c < nC; ++c) {
+      const size_t e = ((size_t)c0 + c) * p.G + g;
+      const double v = s_Q[c][tid];
+      const double m = start ? v : p.W1[a] * v - p.W2[a] * psiM[e];
+      psiM[e] = m;
+      if (nextFin) p.psi_new[((size_t)(a + 1) * p.nc) * p.G + e] = m;
+      for (int f = 0; f < 2; ++f) {
+        const int cfp = s_cfp[team][c][f];
+        if (cfp >= p.nc && s_afp[team][c][f] > 0.0) {
+          const size_t b = (size_t)(cfp - p.nc);
+          p.psiB[((size_t)a * p.nb + b) * p.G + g] = v;
+          if (nextFin) p.psiB[((size_t)(a + 1) * p.nb + b) * p.G + g] = m;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace umt
+
+using namespace umt;
+
+extern "C" {
+
+int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
+  if (!m || !q || ngr < 1 || q->nangles < 2 || !q->omega || !q->weight || !q->angDerivFac || !q->quadTauW1 ||
+      !q->quadTauW2 || !q->starting || !q->finishing || !m->px || !m->cEZ || !m->cFP || !m->numCorner ||
+      !m->cOffSet)
+    return set_error(UMT_ERR_ARG, "umt103_init_rz: null argument or bad sizes");
+  if (m->index_base != 0 && m->index_base != 1) return set_error(UMT_ERR_ARG, "index_base must be 0 or 1");
+  const int nz = m->nzones, nc = m->ncornr, nb = m->nbelem, A = q->nangles, base = m->index_base;
+  if (nz <= 0 || nc <= 0 || nb < 0) return set_error(UMT_ERR_ARG, "bad RZ mesh sizes");
+  for (int zn = 0; zn < nz; ++zn) {
+    if (m->numCorner[zn] < 3 || m->numCorner[zn] > UMT_MAXCORNER)
+      return set_error(UMT_ERR_ARG, "RZ zone %d has %d corners (3..%d supported)", zn, m->numCorner[zn], UMT_MAXCORNER);
+    const int c0 = m->cOffSet[zn];                 // an offset (0-based) in both index conventions
+    if (c0 < 0 || c0 + m->numCorner[zn] > nc) return set_error(UMT_ERR_ARG, "RZ zone %d corner range", zn);
+  }
+  // starting / finishing pattern: every level is start, weighted..., finish
+  int nLevels = 0;
+  std::vector<int> level(A, -1), nextFin(A, 0), start(A, 0);
+  {
+    bool open = false;
+    for (int a = 0; a < A; ++a) {
+      if (q->starting[a]) {
+        if (open) return set_error(UMT_ERR_ARG, "RZ quadrature: level %d has no finishing direction", nLevels - 1);
+        open = true;
+        ++nLevels;
+      }
+      if (!open) return set_error(UMT_ERR_ARG, "RZ quadrature: direction %d outside a level", a);
+      level[a] = nLevels - 1;
+      start[a] = q->starting[a] ? 1 : 0;
+      if (q->finishing[a]) {
+        if (q->starting[a] || a == 0) return set_error(UMT_ERR_ARG, "RZ quadrature: bad finishing direction %d", a);
+        nextFin[a - 1] = 1;
+        open = false;
+      }
+    }
+    if (open) return set_error(UMT_ERR_ARG, "RZ quadrature: last level has no finishing direction");
+  }
+  // 0-based connectivity and the geometry
+  std::vector<int> cez((size_t)nc * 2), cfp((size_t)nc * 2), noff(nz);
+  for (size_t i = 0; i < (size_t)nc * 2; ++i) { cez[i] = m->cEZ[i] - base; cfp[i] = m->cFP[i] - base; }
+  for (int zn = 0; zn < nz; ++zn) noff[zn] = m->cOffSet[zn];
+  for (int zn = 0; zn < nz; ++zn)
+    for (int c = 0; c < m->numCorner[zn]; ++c)
+      for (int f = 0; f < 2; ++f) {
+        const int v = cez[2 * ((size_t)noff[zn] + c) + f];
+        if (v < 0 || v >= m->numCorner[zn]) return set_error(UMT_ERR_ARG, "RZ cEZ out of range at zone %d", zn);
+        const int w = cfp[2 * ((size_t)noff[zn] + c) + f];
+        if (w < 0 || w >= nc + nb) return set_error(UMT_ERR_ARG, "RZ cFP out of range at zone %d", zn);
+      }
+  RZData *r = new RZData();
+  r->hArea.assign(nc, 0.0); r->hVolume.assign(nc, 0.0);
+  r->hRfp.assign((size_t)nc * 2, 0.0); r->hRez.assign((size_t)nc * 2, 0.0);
+  std::vector<double> A_fp, A_ez;
+  geometry_rz(nz, m->numCorner, noff.data(), cez.data(), m->px, A_fp, A_ez, *r);
+  // the shared context: 3-vector geometry (third component 0), FP64 flux
+  std::vector<int> ncf(nc, 2);
+  UmtMesh m3 = {};
+  m3.index_base = base; m3.nzones = nz; m3.ncornr = nc; m3.nbelem = nb; m3.maxcf = 2; m3.maxFaces = m->maxFaces;
+  m3.numCorner = m->numCorner; m3.cOffSet = m->cOffSet; m3.zoneFaces = m->zoneFaces; m3.zoneOpp = m->zoneOpp;
+  m3.faceOpp = m->faceOpp; m3.nCFaces = ncf.data(); m3.cFP = m->cFP; m3.cEZ = m->cEZ; m3.CToFace = m->CToFace;
+  m3.bdyToC = m->bdyToC; m3.px = nullptr; m3.A_fp = A_fp.data(); m3.A_ez = A_ez.data();
+  m3.Volume = r->hVolume.data();
+  std::vector<double> om3((size_t)A * 3, 0.0);
+  for (int a = 0; a < A; ++a) { om3[3 * a] = q->omega[2 * a]; om3[3 * a + 1] = q->omega[2 * a + 1]; }
+  UmtQuad q3 = {A, om3.data(), q->weight};
+  release_current_context();
+  Ctx &c = cur();
+  int rc = init_context(c, &m3, &q3, ngr, 1);
+  if (rc) { delete r; return rc; }
+  c.rz = r;
+  // the schedule must be cycle-free (convex RZ zones have no intra-zone cycles)
+  {
+    std::vector<uint8_t> bad((size_t)A * nz);
+    UMT_CUDA(cudaMemcpy(bad.data(), c.sch.bad, bad.size(), cudaMemcpyDeviceToHost));
+    for (uint8_t v : bad)
+      if (v) return set_error(UMT_ERR_CYCLE, "RZ: the schedule has a lagged zone, not supported");
+  }
+  // stages: levels concurrently, the swept directions of a level back to back
+  std::vector<int> lev((size_t)A * nz), nh(A);
+  UMT_CUDA(cudaMemcpy(lev.data(), c.sch.level, lev.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(nh.data(), c.sch.nHyper, A * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> off(A, 0);
+  int nStages = 0;
+  {
+    std::vector<int> run(nLevels, 0);
+    for (int a = 0; a < A; ++a) {
+      if (q->finishing[a]) continue;
+      off[a] = run[level[a]];
+      run[level[a]] += nh[a];
+      nStages = std::max(nStages, run[level[a]]);
+    }
+  }
+  r->nLevels = nLevels;
+  r->nStages = nStages;
+  r->hCount.assign(nStages, 0);
+  for (int a = 0; a < A; ++a) {
+    if (q->finishing[a]) continue;
+    for (int zn = 0; zn < nz; ++zn) ++r->hCount[off[a] + lev[(size_t)a * nz + zn]];
+  }
+  r->hOffset.assign(nStages, 0);
+  for (int s = 1; s < nStages; ++s) r->hOffset[s] = r->hOffset[s - 1] + r->hCount[s - 1];
+  std::vector<uint32_t> items((size_t)(nStages ? r->hOffset[nStages - 1] + r->hCount[nStages - 1] : 0));
+  {
+    std::vector<int> fill(r->hOffset);
+    for (int a = 0; a < A; ++a) {
+      if (q->finishing[a]) continue;
+      for (int zn = 0; zn < nz; ++zn) {
+        const int s = off[a] + lev[(size_t)a * nz + zn];
+        items[fill[s]++] = (uint32_t)a * (uint32_t)nz + (uint32_t)zn;
+      }
+    }
+  }
+  for (int s = 0; s < nStages; ++s) r->maxStageItems = std::max(r->maxStageItems, r->hCount[s]);
+  rc = upload(&r->items, items.data(), items.size());
+  if (!rc) rc = upload(&r->Area, r->hArea.data(), (size_t)nc);
+  if (!rc) rc = upload(&r->RadiusFP, r->hRfp.data(), (size_t)nc * 2);
+  if (!rc) rc = upload(&r->RadiusEZ, r->hRez.data(), (size_t)nc * 2);
+  if (!rc) rc = upload(&r->angDerivFac, q->angDerivFac, (size_t)A);
+  if (!rc) rc = upload(&r->W1, q->quadTauW1, (size_t)A);
+  if (!rc) rc = upload(&r->W2, q->quadTauW2, (size_t)A);
+  if (!rc) rc = upload(&r->starting, start.data(), (size_t)A);
+  if (!rc) rc = upload(&r->nextFinishing, nextFin.data(), (size_t)A);
+  if (!rc) rc = upload(&r->level, level.data(), (size_t)A);
+  if (!rc) rc = upload(&r->cFP2, cfp.data(), cfp.size());
+  if (!rc) rc = upload(&r->cEZ2, cez.data(), cez.size());
+  if (rc) return rc;
+  if (cudaMalloc((void **)&r->PsiM, (size_t)nLevels * nc * ngr * sizeof(double)) != cudaSuccess)
+    return set_error(UMT_ERR_NOMEM, "RZ: PsiM allocation failed");
+  (void)flags;
+  return 0;
+}
+
+int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double *PsiB_inout) {
+  Ctx &c = cur();
+  if (!c.ready || !c.rz) return set_error(UMT_ERR_STATE, "umt103_init_rz not called");
+  RZData &r = *c.rz;
+  const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
+  else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
+  if (PsiB_inout) UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
+  UMT_CUDA(cudaMemsetAsync(r.PsiM, 0, (size_t)r.nLevels * ncG * 8, c.stream));
+  RZP p;
+  p.nz = c.nz; p.nc = c.nc; p.nb = c.nb; p.G = c.G;
+  p.items = r.items; p.order = c.sch.order;
+  p.numCorner = c.numCorner; p.cOffSet = c.cOffSet; p.cFP2 = r.cFP2; p.cEZ2 = r.cEZ2;
+  p.afp = c.afp64; p.aez = c.aez64;
+  p.Area = r.Area; p.Volume = c.Volume; p.RadiusFP = r.RadiusFP; p.RadiusEZ = r.RadiusEZ;
+  p.Sigt = c.Sigt; p.STotal = c.STotal; p.tau = c.tau;
+  p.angDerivFac = r.angDerivFac; p.W1 = r.W1; p.W2 = r.W2;
+  p.starting = r.starting; p.nextFinishing = r.nextFinishing; p.level = r.level;
+  p.psi_old = c.psi64[c.cur64]; p.psi_new = c.psi64[1 - c.cur64]; p.psiB = c.psiB64; p.PsiM = r.PsiM;
+  int GT = 1;
+  while (GT < c.G && GT < 32) GT *= 2;
+  const int TEAMS = RZ_NT / GT;
+  UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
+  for (int s = 0; s < r.nStages; ++s) {
+    p.stageBegin = r.hOffset[s];
+    p.stageCount = r.hCount[s];
+    const int blocks = (r.hCount[s] + TEAMS - 1) / TEAMS;
+    switch (GT) {
+      case 1: k_sweep_rz<1><<<blocks, RZ_NT, 0, c.stream>>>(p); break;
+      case 2: k_sweep_rz<2><<<blocks, RZ_NT, 0, c.stream>>>(p); break;
+      case 4: k_sweep_rz<4><<<blocks, RZ_NT, 0, c.stream>>>(p); break;
+      case 8: k_sweep_rz<8><<<blocks, RZ_NT, 0, c.stream>>>(p); break;
+      case 16: k_sweep_rz<16><<<blocks, RZ_NT, 0, c.stream>>>(p); break;
+      default: k_sweep_rz<32><<<blocks, RZ_NT, 0, c.stream>>>(p); break;
+    }
+  }
+  UMT_CUDA(cudaGetLastError());
+  // PhiTotal = sum_a w_a psi_a (starting and finishing directions weigh 0)
+  int rc = launch_tally(c, UMT_FP64);
+  if (rc) return rc;
+  UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  cudaEventElapsedTime(&c.lastMs, c.ev0, c.ev1);
+  if (PhiTotal) UMT_CUDA(cudaMemcpy(PhiTotal, c.Phi, ncG * 8, cudaMemcpyDeviceToHost));
+  if (PsiB_inout) UMT_CUDA(cudaMemcpy(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost));
+  if (savePsi) c.cur64 = 1 - c.cur64;
+  return 0;
+}
+
+int umt103_get_geometry_rz(double *Area, double *Volume, double *RadiusFP, double *RadiusEZ) {
+  Ctx &c = cur();
+  if (!c.ready || !c.rz) return set_error(UMT_ERR_STATE, "umt103_init_rz not called");
+  const RZData &r = *c.rz;
+  if (Area) std::copy(r.hArea.begin(), r.hArea.end(), Area);
+  if (Volume) std::copy(r.hVolume.begin(), r.hVolume.end(), Volume);
+  if (RadiusFP) std::copy(r.hRfp.begin(), r.hRfp.end(), RadiusFP);
+  if (RadiusEZ) std::copy(r.hRez.begin(), r.hRez.end(), RadiusEZ);
+  return 0;
+}
+
+}  // extern "C"

@@ -340,6 +340,19 @@ static int enqueue_sweep(Ctx &c, int cur) {
   return 0;
 }
 
+// PhiTotal = sum_a w_a psi_a over the new angular flux (psi[1 - cur]) of the
+// given precision, on the context's stream.
+int launch_tally(Ctx &c, int precision) {
+  const size_t ncG = (size_t)c.nc * c.G;
+  const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
+  if (precision == 1)
+    k_tally32<<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - c.cur32], c.Phi);
+  else
+    k_tally<double><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight, c.psi64[1 - c.cur64], c.Phi);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
 int record_mid(Ctx &c) {
   cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
   UMT_CUDA(cudaStreamIsCapturing(c.stream, &st));

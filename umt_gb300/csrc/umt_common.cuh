@@ -73,6 +73,7 @@ struct Ctx {
   size_t progBytes = 0;
   int progMaxChunks = 0;                        // longest program, 16-byte units
   int progState = 0;                            // 0 not built, 1 built, -1 unavailable
+  struct RZData *rz = nullptr;                  // 2-D RZ problem data (rz.cu), or none
   bool usePDL = true;                           // stage launches as programmatic dependents
   int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
   int *ticket = nullptr;                        // persistent-mode work ticket
@@ -155,6 +156,8 @@ int prepare_sweep32(Ctx &c);
 bool sweep32_supported(int G, int GT, int GPL);
 int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL);
 void default_tile(int G, int *GT, int *GPL);
+// 2-D RZ sweep (rz.cu)
+void free_rz(Ctx &c);
 // zone-program FP32 kernel (sweep32p.cu)
 int prepare_prog32(Ctx &c);
 bool sweep32p_supported(int G, int GT, int GPL);

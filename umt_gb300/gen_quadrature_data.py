@@ -2,7 +2,8 @@
 
 The product-quadrature ordinates and weights of Teton are tabulated numbers
 (mods/QuadratureData_mod.F90:1144-2839: first/last offsets per order, and
-cosTheta / weightTheta / cosPhiXYZ / weightPhiXYZ).  Directions must be
+cosTheta / weightTheta / cosPhiXYZ / weightPhiXYZ, and cosPhiRZ / weightPhiRZ
+for the 2-D RZ product set).  Directions must be
 identical to the reference's for parity, so the tables are extracted
 verbatim as data by this script (run on a machine that has the source tree):
 
@@ -11,7 +12,7 @@ verbatim as data by this script (run on a machine that has the source tree):
 import re
 import sys
 
-NAMES = ["first", "last", "cosTheta", "weightTheta", "cosPhiXYZ", "weightPhiXYZ"]
+NAMES = ["first", "last", "cosTheta", "weightTheta", "cosPhiXYZ", "weightPhiXYZ", "cosPhiRZ", "weightPhiRZ"]
 
 
 def parse(path):
