@@ -223,6 +223,69 @@ def time_to_converge(lib, prob, use_gta=False, tol64=1e-8, tol32=1e-7):
             "tolerance_fp64": tol64, "tolerance_fp32": tol32}
 
 
+def run_rz(args):
+    """2-D RZ sweep (FP64): nr x nz quadrilaterals, RZ product quadrature
+    P = 4, Az = 8 (144 directions), 16 groups.  Device time of the whole
+    sweep (stage kernels + tally) with CUDA events; end to end through
+    umt103_sweep_rz with host buffers; the oracle's RZ sweep on two whole
+    xi-levels of the same mesh as the single-thread CPU baseline."""
+    import torch
+    from umt_gb300 import build, capi
+    from umt_gb300.mesh_rz import build_rz_mesh
+    from umt_gb300.quadrature_rz import product_quadrature_rz
+    build.build()
+    lib = capi.Library()
+    nr = nzr = args.rz_cells
+    m = build_rz_mesh(nr, nzr, distort=0.1, seed=2)
+    q = product_quadrature_rz(4, 8)
+    G = 16
+    A = len(q.weight)
+    rng = np.random.Generator(np.random.Philox(2))
+    sigt = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), size=(m.nzones, G)))
+    STotal = rng.uniform(0.05, 1.0, size=(m.ncornr, G))
+    lib.init_rz(m, q, G)
+    lib.set_materials(sigt, np.zeros_like(sigt), 1.0 / (299.792458 * 1e-3))
+    lib.set_psi(np.full((A, m.ncornr, G), 0.5 / np.pi), None)
+    PsiB = np.zeros((A, m.nbelem, G))
+    units = m.ncornr * A * G
+    for _ in range(args.warmup):
+        lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB)
+    torch.cuda.synchronize()
+    ms, t0 = [], time.perf_counter()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB)
+            ms.append(lib.last_ms())
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    t_dev = sum(ms) / len(ms)
+    line = {"metric": METRIC + " (RZ)", "value": t_dev * 1e6 / units, "unit": "ns", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"RZ sweep, {nr}x{nzr} quadrilaterals, 144 directions, 16 groups",
+                       "zones": m.nzones, "corners": m.ncornr, "directions": A, "groups": G,
+                       "units_per_step": units, "l2": "angular flux %.1f GB" % (units * 8 / 1e9)},
+            "e2e": {"value": t_e2e * 1e9 / units, "unit": "ns",
+                    "h2d_bytes_per_step": STotal.nbytes + PsiB.nbytes, "d2h_bytes_per_step": STotal.nbytes + PsiB.nbytes},
+            "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as po
+        geo = po.geometry_rz(m)
+        keep = np.nonzero(q.level < 2)[0]                      # two whole xi-levels
+        sub = product_quadrature_rz(4, 8)
+        for k in ("omega", "weight", "starting", "finishing", "level", "alpha", "tau", "angDerivFac",
+                  "quadTauW1", "quadTauW2"):
+            setattr(sub, k, getattr(sub, k)[keep])
+        om3 = np.zeros((len(keep), 3)); om3[:, :2] = sub.omega
+        S = po.schedule(m, geo["A_fp"], geo["A_ez"], om3)
+        Psi = np.full((len(keep), m.ncornr, G), 0.5 / np.pi); PB = np.zeros((len(keep), m.nbelem, G))
+        t0 = time.perf_counter()
+        po.set_sweep_rz(m, geo, S, sigt, STotal, 1.0 / (299.792458 * 1e-3), om3, sub, Psi, PB)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": dt * 1e9 / (m.ncornr * len(keep) * G), "unit": "ns", "cores": 1,
+                                "kind": "port", "sample": f"{len(keep)} of {A} directions (two xi-levels), FP64"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -234,9 +297,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
+    ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (FP64)")
+    ap.add_argument("--rz-cells", type=int, default=200, help="RZ mesh: cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
+    if args.rz:
+        if rank == 0:
+            run_rz(args)
+        return
 
     if args.impl == "reference":
         run_reference(args, world, rank)

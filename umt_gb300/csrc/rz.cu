@@ -327,19 +327,43 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
     for (uint8_t v : bad)
       if (v) return set_error(UMT_ERR_CYCLE, "RZ: the schedule has a lagged zone, not supported");
   }
-  // stages: levels concurrently, the swept directions of a level back to back
-  std::vector<int> lev((size_t)A * nz), nh(A);
+  // Stages.  Item (a, z) needs its upwind zones in direction a, and PsiM of
+  // zone z from the previous swept direction of its level:
+  //   stage(a, z) = max(stage(prev(a), z) + 1, stage(a, u) + 1 over upwind u),
+  // so a level's directions follow one another zone by zone (a wavefront
+  // right behind the previous one), and the levels run concurrently.
+  std::vector<int> lev((size_t)A * nz), nh(A), zopp((size_t)nz * UMT_MAXFACES), zfac(nz);
+  std::vector<uint8_t> exm((size_t)A * nz);
   UMT_CUDA(cudaMemcpy(lev.data(), c.sch.level, lev.size() * sizeof(int), cudaMemcpyDeviceToHost));
   UMT_CUDA(cudaMemcpy(nh.data(), c.sch.nHyper, A * sizeof(int), cudaMemcpyDeviceToHost));
-  std::vector<int> off(A, 0);
+  UMT_CUDA(cudaMemcpy(exm.data(), c.sch.exitMask, exm.size(), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(zopp.data(), c.zoneOpp, zopp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(zfac.data(), c.zoneFaces, nz * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> stg((size_t)A * nz, 0);
   int nStages = 0;
   {
-    std::vector<int> run(nLevels, 0);
+    std::vector<int> prevOf(nLevels, -1), byLevel(nz), cnt;
     for (int a = 0; a < A; ++a) {
       if (q->finishing[a]) continue;
-      off[a] = run[level[a]];
-      run[level[a]] += nh[a];
-      nStages = std::max(nStages, run[level[a]]);
+      const int p = prevOf[level[a]];
+      int *sa = stg.data() + (size_t)a * nz;
+      for (int zn = 0; zn < nz; ++zn) sa[zn] = p >= 0 ? stg[(size_t)p * nz + zn] + 1 : 0;
+      // zones in hyperplane order (a topological order of direction a)
+      cnt.assign(nh[a] + 1, 0);
+      for (int zn = 0; zn < nz; ++zn) ++cnt[lev[(size_t)a * nz + zn] + 1];
+      for (int h = 0; h < nh[a]; ++h) cnt[h + 1] += cnt[h];
+      for (int zn = 0; zn < nz; ++zn) byLevel[cnt[lev[(size_t)a * nz + zn]]++] = zn;
+      for (int i = 0; i < nz; ++i) {
+        const int zn = byLevel[i];
+        const uint8_t mask = exm[(size_t)a * nz + zn];
+        for (int f = 0; f < zfac[zn]; ++f)
+          if (mask & (1u << f)) {
+            const int d = zopp[(size_t)zn * UMT_MAXFACES + f];
+            if (d >= 0) sa[d] = std::max(sa[d], sa[zn] + 1);
+          }
+      }
+      for (int zn = 0; zn < nz; ++zn) nStages = std::max(nStages, sa[zn] + 1);
+      prevOf[level[a]] = a;
     }
   }
   r->nLevels = nLevels;
@@ -347,7 +371,7 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
   r->hCount.assign(nStages, 0);
   for (int a = 0; a < A; ++a) {
     if (q->finishing[a]) continue;
-    for (int zn = 0; zn < nz; ++zn) ++r->hCount[off[a] + lev[(size_t)a * nz + zn]];
+    for (int zn = 0; zn < nz; ++zn) ++r->hCount[stg[(size_t)a * nz + zn]];
   }
   r->hOffset.assign(nStages, 0);
   for (int s = 1; s < nStages; ++s) r->hOffset[s] = r->hOffset[s - 1] + r->hCount[s - 1];
@@ -356,10 +380,7 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
     std::vector<int> fill(r->hOffset);
     for (int a = 0; a < A; ++a) {
       if (q->finishing[a]) continue;
-      for (int zn = 0; zn < nz; ++zn) {
-        const int s = off[a] + lev[(size_t)a * nz + zn];
-        items[fill[s]++] = (uint32_t)a * (uint32_t)nz + (uint32_t)zn;
-      }
+      for (int zn = 0; zn < nz; ++zn) items[fill[stg[(size_t)a * nz + zn]]++] = (uint32_t)a * (uint32_t)nz + (uint32_t)zn;
     }
   }
   for (int s = 0; s < nStages; ++s) r->maxStageItems = std::max(r->maxStageItems, r->hCount[s]);
