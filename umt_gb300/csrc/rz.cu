@@ -9,11 +9,12 @@
 // The corner-face vectors are 2-vectors; they are stored as 3-vectors with a
 // zero third component, so the device schedule of the 3-D path (face-sign
 // dependencies, corner order, hyperplane levels) orders every RZ direction
-// unchanged.  Stages: the levels run concurrently, the directions of a level
-// back to back, so the item (direction a, zone z) of level L sits at stage
-// offset(a) + hyperplane(a, z), offset(a) being the hyperplanes of the
-// level's earlier swept directions.  One kernel launch per stage; a team of
-// GT lanes per item, lanes over groups, as in the FP64 kernel of sweep.cu.
+// unchanged.  Stages: item (direction a, zone z) waits for its upwind zones
+// in direction a and for zone z in the level's previous swept direction (the
+// only reader of the PsiM that one leaves), so a level's directions follow one
+// another as wavefronts one stage apart and the levels run concurrently.  One
+// kernel launch per stage; a team of GT lanes per item, lanes over groups, as
+// in the FP64 kernel of sweep.cu.
 #include "umt_common.cuh"
 #include "../../include/umt103.h"
 
