@@ -224,11 +224,12 @@ def time_to_converge(lib, prob, use_gta=False, tol64=1e-8, tol32=1e-7):
 
 
 def run_rz(args):
-    """2-D RZ sweep (FP64): nr x nz quadrilaterals, RZ product quadrature
-    P = 4, Az = 8 (144 directions), 16 groups.  Device time of the whole
-    sweep (stage kernels + tally) with CUDA events; end to end through
-    umt103_sweep_rz with host buffers; the oracle's RZ sweep on two whole
-    xi-levels of the same mesh as the single-thread CPU baseline."""
+    """2-D RZ sweep (--precision, FP32 by default): nr x nz quadrilaterals,
+    RZ product quadrature P = 4, Az = 8 (144 directions), 16 groups.  Device
+    time of the whole sweep (stage kernels + tally) with CUDA events; end to
+    end through umt103_sweep_rz with host buffers; the oracle's FP64 RZ sweep
+    on two whole xi-levels of the same mesh as the single-thread CPU
+    baseline."""
     import torch
     from umt_gb300 import build, capi
     from umt_gb300.mesh_rz import build_rz_mesh
@@ -243,27 +244,30 @@ def run_rz(args):
     rng = np.random.Generator(np.random.Philox(2))
     sigt = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), size=(m.nzones, G)))
     STotal = rng.uniform(0.05, 1.0, size=(m.ncornr, G))
-    lib.init_rz(m, q, G)
+    prec = capi.UMT_FP32 if args.precision == "fp32" else capi.UMT_FP64
+    lib.init_rz(m, q, G, flags=2 if prec == capi.UMT_FP32 else 1)
     lib.set_materials(sigt, np.zeros_like(sigt), 1.0 / (299.792458 * 1e-3))
     lib.set_psi(np.full((A, m.ncornr, G), 0.5 / np.pi), None)
     PsiB = np.zeros((A, m.nbelem, G))
     units = m.ncornr * A * G
     for _ in range(args.warmup):
-        lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB)
+        lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB, precision=prec)
     torch.cuda.synchronize()
     ms, t0 = [], time.perf_counter()
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
-            lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB)
+            lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB, precision=prec)
             ms.append(lib.last_ms())
     t_e2e = (time.perf_counter() - t0) / args.steps
     t_dev = sum(ms) / len(ms)
     line = {"metric": METRIC + " (RZ)", "value": t_dev * 1e6 / units, "unit": "ns", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == capi.UMT_FP32 else "f64",
+            "data": "synthetic",
             "config": {"workload": f"RZ sweep, {nr}x{nzr} quadrilaterals, 144 directions, 16 groups",
                        "zones": m.nzones, "corners": m.ncornr, "directions": A, "groups": G,
-                       "units_per_step": units, "l2": "angular flux %.1f GB" % (units * 8 / 1e9)},
+                       "units_per_step": units, "psi": args.precision, "tallies": "fp64",
+                       "l2": "angular flux %.2f GB per buffer" % (units * (4 if prec == capi.UMT_FP32 else 8) / 1e9)},
             "e2e": {"value": t_e2e * 1e9 / units, "unit": "ns",
                     "h2d_bytes_per_step": STotal.nbytes + PsiB.nbytes, "d2h_bytes_per_step": STotal.nbytes + PsiB.nbytes},
             "clocks": clk.summary()}

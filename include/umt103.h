@@ -255,14 +255,17 @@ typedef struct UmtQuadRZ {
 /* Replaces the current context with an RZ problem: geometry (A_fp, A_ez,
  * Area, Volume, RadiusFP, RadiusEZ) and every direction's schedule are built
  * here; the directions of a level are swept in order (each needs the previous
- * one's PsiM), the levels concurrently. */
+ * one's PsiM), the levels concurrently.  flags: bit0 = FP64 angular flux,
+ * bit1 = FP32 angular flux (0 = both), as for umt103_init; the FP32 path
+ * needs ncornr + nbelem < 2^28. */
 int umt103_init_rz(const UmtMeshRZ *mesh, const UmtQuadRZ *quad, int ngr, int flags);
 
 /* One SetSweep of the RZ problem (snac/SetSweep.F90 with SweepUCBrz): same
- * arguments as umt103_sweep, FP64.  Finishing directions receive PsiM, as in
- * the reference.  umt103_set_materials / umt103_set_psi / umt103_get_psi
- * apply to the RZ context as to a 3-D one. */
-int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double *PsiB_inout);
+ * arguments as umt103_sweep.  UMT_FP64 follows the reference's operation
+ * order; UMT_FP32 keeps the flux in FP32 (tallies in FP64).  Finishing
+ * directions receive PsiM, as in the reference.  umt103_set_materials /
+ * umt103_set_psi / umt103_get_psi apply to the RZ context as to a 3-D one. */
+int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double *PsiB_inout, int precision);
 
 /* Copy out the RZ geometry: Area, Volume [ncornr], RadiusFP, RadiusEZ
  * [ncornr*2] (any pointer may be NULL). */

@@ -75,6 +75,71 @@ def test_rz_repeated_sweeps_and_source_iteration(umtlib):
         assert rel_err(PB_d, PB_o) < 1e-12
 
 
+# FP32 RZ sweep: the flux is kept in FP32 (approximate reciprocals, the EZ
+# closure divided through by aez^4) and the tallies in FP64.  Stated
+# tolerance: 2e-5 relative (max-norm) on PhiTotal, 1e-4 on Psi and PsiB.
+FP32_PHI_TOL, FP32_PSI_TOL = 2e-5, 1e-4
+
+
+@pytest.mark.parametrize("nr,nzr,P,Az,G,index_base", [(6, 5, 4, 3, 8, 0), (7, 6, 2, 4, 16, 1), (3, 4, 1, 2, 3, 0)])
+def test_rz_fp32_sweep_matches_oracle(umtlib, nr, nzr, P, Az, G, index_base):
+    m, q, sigt, STotal, psi0, PsiB = _problem(nr, nzr, P, Az, G, seed=nr * 7 + G)
+    tau = 0.7
+    geo, Phi_ref, Psi_ref, PsiB_ref = _oracle(m, q, sigt, STotal, psi0, PsiB, tau)
+    umtlib.init_rz(m, q, G, index_base=index_base)
+    umtlib.set_materials(sigt, np.zeros_like(sigt), tau)
+    umtlib.set_psi(psi0, None)
+    PB = PsiB.copy()
+    Phi = umtlib.sweep_rz(STotal, savePsi=True, PsiB=PB, precision=capi.UMT_FP32)
+    Psi, _ = umtlib.get_psi(capi.UMT_FP32)
+    assert rel_err(Phi, Phi_ref) < FP32_PHI_TOL
+    assert rel_err(Psi, Psi_ref) < FP32_PSI_TOL
+    assert rel_err(PB, PsiB_ref) < FP32_PSI_TOL
+
+
+def test_rz_fp32_repeated_sweeps_and_tau_change(umtlib):
+    """FP32 sweeps replayed from graphs of both buffer parities, and captured
+    again after tau changes, stay within the FP32 tolerance of the oracle."""
+    m, q, sigt, STotal, psi0, PsiB = _problem(5, 6, 2, 3, 16, seed=11)
+    from oracle import pyoracle as po
+    geo = po.geometry_rz(m)
+    om3 = np.zeros((len(q.weight), 3)); om3[:, :2] = q.omega
+    S = po.schedule(m, geo["A_fp"], geo["A_ez"], om3)
+    umtlib.init_rz(m, q, 16)
+    umtlib.set_psi(psi0, None)
+    Psi_o = psi0.copy()
+    for tau, save in ((0.3, True), (0.3, False), (0.3, True), (1.1, True), (1.1, True)):
+        umtlib.set_materials(sigt, np.zeros_like(sigt), tau)
+        PB_o = PsiB.copy(); PB_d = PsiB.copy()
+        Phi_o = po.set_sweep_rz(m, geo, S, sigt, STotal, tau, om3, q, Psi_o, PB_o, savePsi=save)
+        Phi_d = umtlib.sweep_rz(STotal, savePsi=save, PsiB=PB_d, precision=capi.UMT_FP32)
+        assert rel_err(Phi_d, Phi_o) < FP32_PHI_TOL
+        assert rel_err(PB_d, PB_o) < FP32_PSI_TOL
+    Psi_d, _ = umtlib.get_psi(capi.UMT_FP32)
+    assert rel_err(Psi_d, Psi_o) < FP32_PSI_TOL
+
+
+def test_rz_precision_refusals(umtlib):
+    m, q, sigt, STotal, psi0, PsiB = _problem(2, 3, 1, 1, 2, seed=4)
+    umtlib.init_rz(m, q, 2, flags=1)                     # FP64 flux only
+    umtlib.set_materials(sigt, np.zeros_like(sigt), 0.5)
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.sweep_rz(STotal, precision=capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_STATE
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.sweep_rz(STotal, precision=7)
+    assert e.value.code == capi.UMT_ERR_ARG
+    umtlib.init_rz(m, q, 2, flags=2)                     # FP32 flux only
+    umtlib.set_materials(sigt, np.zeros_like(sigt), 0.5)
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.sweep_rz(STotal, precision=capi.UMT_FP64)
+    assert e.value.code == capi.UMT_ERR_STATE
+    assert np.isfinite(umtlib.sweep_rz(STotal, precision=capi.UMT_FP32)).all()
+    with pytest.raises(capi.UmtError) as e:              # the 3-D sweep refuses an RZ context
+        umtlib.sweep(STotal, precision=capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_STATE
+
+
 def test_rz_errors(umtlib):
     m, q, sigt, STotal, psi0, PsiB = _problem(2, 2, 1, 1, 2, seed=1)
     bad = product_quadrature_rz(1, 1)

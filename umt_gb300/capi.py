@@ -301,9 +301,10 @@ class Library:
         return afp, aez, vol
 
     # ---- 2-D RZ geometry ----
-    def init_rz(self, mesh, quad, ngr, index_base=0):
+    def init_rz(self, mesh, quad, ngr, index_base=0, flags=0):
         """umt103_init_rz with a umt_gb300.mesh_rz.MeshRZ and a
-        umt_gb300.quadrature_rz.QuadRZ."""
+        umt_gb300.quadrature_rz.QuadRZ; flags as for umt103_init (0: FP64
+        and FP32 angular flux)."""
         m = mesh
         a = dict(numCorner=_c(m.numCorner, np.int32), cOffSet=_c(m.cOffSet, np.int32),
                  zoneFaces=_c(m.zoneFaces, np.int32), zoneOpp=_c(m.zoneOpp, np.int32),
@@ -325,16 +326,17 @@ class Library:
         qs = UmtQuadRZ(len(q.weight), _d(arrs[0]), _d(arrs[1]), _d(arrs[2]), _d(arrs[3]), _d(arrs[4]),
                        _i(arrs[5]), _i(arrs[6]))
         self._keep = [a, px, arrs]
-        check(self.lib.umt103_init_rz(C.byref(st), C.byref(qs), int(ngr), 0))
+        check(self.lib.umt103_init_rz(C.byref(st), C.byref(qs), int(ngr), int(flags)))
         self.A, self.G, self.nz, self.nc, self.nb = len(q.weight), int(ngr), m.nzones, m.ncornr, m.nbelem
         return self
 
-    def sweep_rz(self, STotal=None, savePsi=False, PsiB=None):
+    def sweep_rz(self, STotal=None, savePsi=False, PsiB=None, precision=UMT_FP64):
+        """umt103_sweep_rz; returns PhiTotal, PsiB is updated in place."""
         STotal = _c(STotal, np.float64)
         Phi = np.zeros((self.nc, self.G))
         if PsiB is not None:
             assert PsiB.dtype == np.float64 and PsiB.flags.c_contiguous
-        check(self.lib.umt103_sweep_rz(_d(STotal), int(bool(savePsi)), _d(Phi), _d(PsiB)))
+        check(self.lib.umt103_sweep_rz(_d(STotal), int(bool(savePsi)), _d(Phi), _d(PsiB), int(precision)))
         return Phi
 
     def geometry_rz(self):

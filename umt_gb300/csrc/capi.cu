@@ -153,6 +153,10 @@ int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
       rc = set_error(UMT_ERR_ARG, "batch: context %d not initialised", id);
       break;
     }
+    if (g_ctx[id]->rz) {
+      rc = set_error(UMT_ERR_STATE, "batch: context %d holds an RZ problem (umt103_sweep_rz)", id);
+      break;
+    }
     g_cur = g_ctx[id];
     cudaGraph_t gr = nullptr;
     rc = capture_sweep_graph(*g_cur, precision, &gr);
@@ -458,6 +462,7 @@ int umt103_set_source(const double *STotal) {
 
 static int sweep_core(int savePsi, int precision) {
   Ctx &c = cur();
+  if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem: use umt103_sweep_rz");
   if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
@@ -512,6 +517,7 @@ static int staging64(Ctx &c, size_t n, double **out) {
 int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double *PsiB_inout, int precision) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem: use umt103_sweep_rz");
   if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
@@ -681,6 +687,7 @@ static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps) {
 int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem: use umt103_sweep_rz");
   if (!prm || !res) return set_error(UMT_ERR_ARG, "null params/result");
   const int prec = prm->precision;
   if (prec != UMT_FP64 && prec != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
@@ -788,5 +795,6 @@ int init_context(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags)
   return init_ctx(c, m, q, ngr, flags);
 }
 void release_current_context() { free_all(); }
+int staging_buffer64(Ctx &c, size_t n, double **out) { return staging64(c, n, out); }
 
 }  // namespace umt

@@ -16,10 +16,13 @@
 // kernel launch per stage; a team of GT lanes per item, lanes over groups, as
 // in the FP64 kernel of sweep.cu.
 #include "umt_common.cuh"
+#include "sweep32_util.cuh"
 #include "../../include/umt103.h"
 
 #include <algorithm>
 #include <cmath>
+
+#define TRY_RC(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
 
 namespace umt {
 
@@ -36,14 +39,30 @@ struct RZData {
   int nLevels = 0, nStages = 0, maxStageItems = 0;
   std::vector<int> hCount, hOffset;
   std::vector<double> hArea, hVolume, hRfp, hRez;
+  // FP32 path (init flag bit 1)
+  float4 *recA = nullptr, *recB = nullptr;   // [A][nc] per (direction, corner), see k_rz_prep32
+  float4 *corner32 = nullptr;                // [nc] {Volume, RadiusEZ0*Area, RadiusEZ1*Area, Area}
+  int2 *link32 = nullptr;                    // [nc] {cFP0 << 3 | cEZ0, cFP1 << 3 | cEZ1}
+  float *fac32 = nullptr, *W1_32 = nullptr, *W2_32 = nullptr;   // [A]
+  float *PsiM32 = nullptr;                   // [nLevels][nc][G]
+  cudaGraphExec_t graph32[2] = {nullptr, nullptr};   // one FP32 sweep per buffer parity
+  double graphTau = 0.0;
 };
+
+static void destroy_rz_graphs(RZData &r) {
+  for (auto &g : r.graph32)
+    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
 
 void free_rz(Ctx &c) {
   RZData *r = c.rz;
   if (!r) return;
+  destroy_rz_graphs(*r);
   for (void *p : {(void *)r->Area, (void *)r->RadiusFP, (void *)r->RadiusEZ, (void *)r->angDerivFac, (void *)r->W1,
                   (void *)r->W2, (void *)r->starting, (void *)r->nextFinishing, (void *)r->level, (void *)r->cFP2,
-                  (void *)r->cEZ2, (void *)r->PsiM, (void *)r->items})
+                  (void *)r->cEZ2, (void *)r->PsiM, (void *)r->items, (void *)r->recA, (void *)r->recB,
+                  (void *)r->corner32, (void *)r->link32, (void *)r->fac32, (void *)r->W1_32, (void *)r->W2_32,
+                  (void *)r->PsiM32})
     if (p) cudaFree(p);
   delete r;
   c.rz = nullptr;
@@ -246,6 +265,261 @@ __global__ void __launch_bounds__(RZ_NT) k_sweep_rz(RZP p) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 RZ sweep.
+//
+// Per (direction, corner) the FP32 kernel reads two records built once from
+// the FP64 projections the schedule was decided with, so every face is
+// classified exactly as the schedule classified it:
+//   recA = {RadiusFP0*afp0, RadiusFP1*afp1, RadiusEZ0*aez0, RadiusEZ1*aez1}
+//   recB = {sumArea, Area/aez0, Area/aez1, face bits}
+// with sumArea = angDerivFac*Area + sum of RadiusFP*|afp| over incoming FP
+// faces + RadiusEZ*aez over the EZ faces that feed the corner, and face bits
+// 1<<f (afp_f < 0, incoming), 4<<f (afp_f > 0, exiting), 16<<f (aez_f > 0).
+// One thread per (direction, zone); sums in FP64, rounded once.
+__global__ void k_rz_prep32(int A, int nz, int nc, const int *numCorner, const int *cOffSet, const int *cEZ2,
+                            const double *afp, const double *aez, const double *Area, const double *Rfp,
+                            const double *Rez, const double *angDerivFac, float4 *recA, float4 *recB) {
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)A * nz) return;
+  const int a = (int)(t / (size_t)nz), z = (int)(t - (size_t)a * nz);
+  const int nC = numCorner[z], c0 = cOffSet[z];
+  const size_t abase = (size_t)a * nc;
+  const double fac = angDerivFac[a];
+  double sum[RZ_MAXC];
+  for (int c = 0; c < nC; ++c) sum[c] = fac * Area[c0 + c];
+  for (int c = 0; c < nC; ++c)
+    for (int f = 0; f < 2; ++f) {
+      const size_t cc = (size_t)c0 + c;
+      const double fp = afp[(abase + cc) * UMT_MAXCF + f], ez = aez[(abase + cc) * UMT_MAXCF + f];
+      if (fp < 0.0) sum[c] -= Rfp[2 * cc + f] * fp;
+      if (ez > 0.0) sum[cEZ2[2 * cc + f]] += Rez[2 * cc + f] * ez;
+    }
+  for (int c = 0; c < nC; ++c) {
+    const size_t cc = (size_t)c0 + c;
+    double fp[2], ez[2];
+    unsigned bits = 0;
+    for (int f = 0; f < 2; ++f) {
+      fp[f] = afp[(abase + cc) * UMT_MAXCF + f];
+      ez[f] = aez[(abase + cc) * UMT_MAXCF + f];
+      if (fp[f] < 0.0) bits |= 1u << f;
+      if (fp[f] > 0.0) bits |= 4u << f;
+      if (ez[f] > 0.0) bits |= 16u << f;
+    }
+    recA[abase + cc] = make_float4((float)(Rfp[2 * cc] * fp[0]), (float)(Rfp[2 * cc + 1] * fp[1]),
+                                   (float)(Rez[2 * cc] * ez[0]), (float)(Rez[2 * cc + 1] * ez[1]));
+    recB[abase + cc] = make_float4((float)sum[c], ez[0] > 0.0 ? (float)(Area[cc] / ez[0]) : 0.f,
+                                   ez[1] > 0.0 ? (float)(Area[cc] / ez[1]) : 0.f, __uint_as_float(bits));
+  }
+}
+
+__global__ void k_rz_to_float(size_t n, const double *x, float *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (float)x[i];
+}
+
+__global__ void k_rz_to_double(size_t n, const float *x, double *y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = (double)x[i];
+}
+
+struct RZP32 {
+  int nz, nc, nb, G;
+  const uint32_t *items;
+  int stageBegin, stageCount;
+  const uint32_t *order;
+  const int *numCorner, *cOffSet;
+  const float4 *recA, *recB, *corner;
+  const int2 *link;
+  const float *Sigt, *STotal;
+  float tau;
+  const float *fac, *W1, *W2;
+  const int *starting, *nextFinishing, *level;
+  const float *psi_old;
+  float *psi_new, *psiB, *PsiM;
+};
+
+// One dependency stage of the FP32 RZ sweep: a team of GT lanes per
+// (direction, zone), lanes over groups; the operations of k_sweep_rz in the
+// same order, with the EZ closure of a corner face whose FP face is incoming
+// divided through by aez^4 (x = sigma*Area/aez):
+//   sez = RadiusEZ*Area (N (sigma psi_fp - Q_c) + D (Q_c - Q_z)) / (N + 2 x D),
+//   N = 1.82 x^2 + 4 x + 3,  D = 2 x^3 + 3 x^2 + 2 x + 1,
+// algebraically the reference's gnum/gden form; x is capped at 1e8 so every
+// term stays finite in FP32.  Divisions are approximate reciprocals times a
+// multiply.  Programmatic dependent launch: everything before pdl_wait()
+// reads only data no stage writes.
+template <int GT>
+__global__ void __launch_bounds__(RZ_NT) k_sweep_rz32(RZP32 p) {
+  pdl_launch_dependents();
+  constexpr int TEAMS = RZ_NT / GT;
+  __shared__ float s_src[RZ_MAXC][RZ_NT], s_Q[RZ_MAXC][RZ_NT], s_pm[RZ_MAXC][RZ_NT];
+  __shared__ float4 s_A[TEAMS][RZ_MAXC], s_B[TEAMS][RZ_MAXC], s_C[TEAMS][RZ_MAXC];
+  __shared__ int2 s_L[TEAMS][RZ_MAXC];
+  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
+  const int k = blockIdx.x * TEAMS + team;
+  if (k >= p.stageCount) return;                       // whole teams leave together
+  const unsigned teammask = team_mask(GT, tid);
+  const uint32_t it = p.items[p.stageBegin + k];
+  const int a = (int)(it / (uint32_t)p.nz);
+  const int z = (int)(it - (uint32_t)a * p.nz);
+  const int nC = p.numCorner[z], c0 = p.cOffSet[z];
+  const uint32_t ord = p.order[it];
+  const size_t abase = (size_t)a * p.nc;
+  for (int c = lane; c < nC; c += GT) {
+    s_A[team][c] = p.recA[abase + c0 + c];
+    s_B[team][c] = p.recB[abase + c0 + c];
+    s_C[team][c] = p.corner[c0 + c];
+    s_L[team][c] = p.link[c0 + c];
+  }
+  const float fac = p.fac[a], W1 = p.W1[a], W2 = p.W2[a];
+  const bool start = p.starting[a] != 0, nextFin = p.nextFinishing[a] != 0;
+  float *psiM = p.PsiM + (size_t)p.level[a] * p.nc * p.G;
+  __syncwarp(teammask);
+  pdl_wait();
+  for (int g = lane; g < p.G; g += GT) {
+    const float sig = p.Sigt[(size_t)z * p.G + g];
+    float po[RZ_MAXC], st[RZ_MAXC], pu[RZ_MAXC][2];
+#pragma unroll
+    for (int c = 0; c < RZ_MAXC; ++c) {
+      po[c] = st[c] = pu[c][0] = pu[c][1] = 0.f;
+      if (c < nC) {
+        const size_t e = ((size_t)c0 + c) * p.G + g;
+        po[c] = p.psi_old[abase * p.G + e];
+        st[c] = p.STotal[e];
+        s_pm[c][tid] = psiM[e];
+        const unsigned bits = __float_as_uint(s_B[team][c].w);
+        const int2 L = s_L[team][c];
+#pragma unroll
+        for (int f = 0; f < 2; ++f)
+          if (bits & (1u << f)) {
+            const int cfp = (f ? L.y : L.x) >> 3;
+            pu[c][f] = cfp < p.nc ? p.psi_new[(abase + cfp) * p.G + g]
+                                  : p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g];
+          }
+      }
+    }
+    const float rsig = rcp_approx(sig);
+#pragma unroll
+    for (int c = 0; c < RZ_MAXC; ++c)
+      if (c < nC) {
+        const float q = fmaf(p.tau, po[c], st[c]);
+        s_Q[c][tid] = q;
+        s_src[c][tid] = s_C[team][c].x * q;
+      }
+#pragma unroll
+    for (int c = 0; c < RZ_MAXC; ++c) {
+      if (c >= nC) continue;
+      const float4 A = s_A[team][c], B = s_B[team][c], C = s_C[team][c];
+      const unsigned bits = __float_as_uint(B.w);
+      const int2 L = s_L[team][c];
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+        const float kfp = f ? A.y : A.x, rae = f ? A.w : A.z, xa = f ? B.z : B.y, rza = f ? C.z : C.y;
+        if (bits & (1u << f)) s_src[c][tid] = fmaf(-kfp, pu[c][f], s_src[c][tid]);
+        if (bits & (16u << f)) {
+          const int cez = (f ? L.y : L.x) & 7;
+          const float Qc = s_Q[c][tid], Qz = s_Q[cez][tid];
+          float sez;
+          if (bits & (1u << f)) {
+            const float x = fminf(sig * xa, 1e8f);
+            const float N = fmaf(fmaf(1.82f, x, 4.f), x, 3.f);
+            const float D = fmaf(fmaf(fmaf(2.f, x, 3.f), x, 2.f), x, 1.f);
+            sez = rza * fmaf(N, fmaf(sig, pu[c][f], -Qc), D * (Qc - Qz)) * rcp_approx(fmaf(2.f * x, D, N));
+          } else {
+            sez = 0.5f * rae * (Qc - Qz) * rsig;
+          }
+          s_src[c][tid] += sez;
+          s_src[cez][tid] -= sez;
+        }
+      }
+    }
+    float *out = p.psi_new + abase * p.G;
+#pragma unroll
+    for (int i = 0; i < RZ_MAXC; ++i) {
+      if (i >= nC) continue;
+      const int c = (int)((ord >> (4 * i)) & 15u);
+      const float4 B = s_B[team][c], C = s_C[team][c], A = s_A[team][c];
+      const int2 L = s_L[team][c];
+      const float v = fmaf(C.w * fac, s_pm[c][tid], s_src[c][tid]) * rcp_approx(fmaf(sig, C.x, B.x));
+      out[((size_t)c0 + c) * p.G + g] = v;
+      s_Q[c][tid] = v;                       // Q is no longer needed: keep the solved flux
+      const unsigned bits = __float_as_uint(B.w);
+      if (bits & 16u) s_src[L.x & 7][tid] = fmaf(A.z, v, s_src[L.x & 7][tid]);
+      if (bits & 32u) s_src[L.y & 7][tid] = fmaf(A.w, v, s_src[L.y & 7][tid]);
+    }
+#pragma unroll
+    for (int c = 0; c < RZ_MAXC; ++c) {
+      if (c >= nC) continue;
+      const size_t e = ((size_t)c0 + c) * p.G + g;
+      const float v = s_Q[c][tid];
+      const float m = start ? v : fmaf(W1, v, -W2 * s_pm[c][tid]);
+      psiM[e] = m;
+      if (nextFin) p.psi_new[(abase + p.nc) * p.G + e] = m;
+      const unsigned bits = __float_as_uint(s_B[team][c].w);
+      const int2 L = s_L[team][c];
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+        const int cfp = (f ? L.y : L.x) >> 3;
+        if ((bits & (4u << f)) && cfp >= p.nc) {
+          const size_t b = (size_t)(cfp - p.nc);
+          p.psiB[((size_t)a * p.nb + b) * p.G + g] = v;
+          if (nextFin) p.psiB[((size_t)(a + 1) * p.nb + b) * p.G + g] = m;
+        }
+      }
+    }
+  }
+}
+
+// Launch every stage of one FP32 RZ sweep (conversions, PsiM reset, stages,
+// tally) on the context's stream; stages after the first carry the
+// programmatic-serialization attribute.
+static int enqueue_sweep_rz32(Ctx &c, RZData &r) {
+  const size_t ncG = (size_t)c.nc * c.G, nzG = (size_t)c.nz * c.G;
+  k_rz_to_float<<<(int)std::min<size_t>((nzG + 255) / 256, 4096), 256, 0, c.stream>>>(nzG, c.Sigt, c.Sigt32);
+  k_rz_to_float<<<(int)std::min<size_t>((ncG + 255) / 256, 4096), 256, 0, c.stream>>>(ncG, c.STotal, c.STotal32);
+  UMT_CUDA(cudaMemsetAsync(r.PsiM32, 0, (size_t)r.nLevels * ncG * sizeof(float), c.stream));
+  RZP32 p;
+  p.nz = c.nz; p.nc = c.nc; p.nb = c.nb; p.G = c.G;
+  p.items = r.items; p.order = c.sch.order;
+  p.numCorner = c.numCorner; p.cOffSet = c.cOffSet;
+  p.recA = r.recA; p.recB = r.recB; p.corner = r.corner32; p.link = r.link32;
+  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
+  p.fac = r.fac32; p.W1 = r.W1_32; p.W2 = r.W2_32;
+  p.starting = r.starting; p.nextFinishing = r.nextFinishing; p.level = r.level;
+  p.psi_old = c.psi32[c.cur32]; p.psi_new = c.psi32[1 - c.cur32]; p.psiB = c.psiB32; p.PsiM = r.PsiM32;
+  int GT = 1;
+  while (GT < c.G && GT < 32) GT *= 2;
+  const int TEAMS = RZ_NT / GT;
+  void (*kern)(RZP32) = nullptr;
+  switch (GT) {
+    case 1: kern = k_sweep_rz32<1>; break;
+    case 2: kern = k_sweep_rz32<2>; break;
+    case 4: kern = k_sweep_rz32<4>; break;
+    case 8: kern = k_sweep_rz32<8>; break;
+    case 16: kern = k_sweep_rz32<16>; break;
+    default: kern = k_sweep_rz32<32>; break;
+  }
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  bool first = true;
+  for (int s = 0; s < r.nStages; ++s) {
+    if (r.hCount[s] == 0) continue;
+    p.stageBegin = r.hOffset[s];
+    p.stageCount = r.hCount[s];
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((r.hCount[s] + TEAMS - 1) / TEAMS));
+    cfg.blockDim = dim3(RZ_NT);
+    cfg.stream = c.stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = first ? 0 : 1;            // the first stage follows the conversions in full
+    first = false;
+    UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p));
+  }
+  return launch_tally(c, UMT_FP32);
+}
+
 }  // namespace umt
 
 using namespace umt;
@@ -316,9 +590,14 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
   std::vector<double> om3((size_t)A * 3, 0.0);
   for (int a = 0; a < A; ++a) { om3[3 * a] = q->omega[2 * a]; om3[3 * a + 1] = q->omega[2 * a + 1]; }
   UmtQuad q3 = {A, om3.data(), q->weight};
+  const int precFlags = (flags & 3) ? (flags & 3) : 3;     // bit 0: FP64 flux, bit 1: FP32 flux
+  if ((precFlags & 2) && (long long)nc + nb >= (1LL << 28)) {
+    delete r;
+    return set_error(UMT_ERR_ARG, "RZ FP32 path: ncornr + nbelem must be below 2^28");
+  }
   release_current_context();
   Ctx &c = cur();
-  int rc = init_context(c, &m3, &q3, ngr, 1);
+  int rc = init_context(c, &m3, &q3, ngr, precFlags);
   if (rc) { delete r; return rc; }
   c.rz = r;
   // the schedule must be cycle-free (convex RZ zones have no intra-zone cycles)
@@ -398,19 +677,96 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
   if (!rc) rc = upload(&r->cFP2, cfp.data(), cfp.size());
   if (!rc) rc = upload(&r->cEZ2, cez.data(), cez.size());
   if (rc) return rc;
-  if (cudaMalloc((void **)&r->PsiM, (size_t)nLevels * nc * ngr * sizeof(double)) != cudaSuccess)
+  if ((c.flags & 1) && cudaMalloc((void **)&r->PsiM, (size_t)nLevels * nc * ngr * sizeof(double)) != cudaSuccess)
     return set_error(UMT_ERR_NOMEM, "RZ: PsiM allocation failed");
-  (void)flags;
+  if (c.flags & 2) {
+    std::vector<float4> corner(nc);
+    std::vector<int2> link(nc);
+    for (int cc = 0; cc < nc; ++cc) {
+      const double ar = r->hArea[cc];
+      corner[cc] = make_float4((float)r->hVolume[cc], (float)(r->hRez[2 * cc] * ar), (float)(r->hRez[2 * cc + 1] * ar),
+                               (float)ar);
+      link[cc] = make_int2(cfp[2 * (size_t)cc] << 3 | cez[2 * (size_t)cc], cfp[2 * (size_t)cc + 1] << 3 | cez[2 * (size_t)cc + 1]);
+    }
+    std::vector<float> fac(A), w1(A), w2(A);
+    for (int a = 0; a < A; ++a) {
+      fac[a] = (float)q->angDerivFac[a]; w1[a] = (float)q->quadTauW1[a]; w2[a] = (float)q->quadTauW2[a];
+    }
+    rc = upload(&r->corner32, corner.data(), (size_t)nc);
+    if (!rc) rc = upload(&r->link32, link.data(), (size_t)nc);
+    if (!rc) rc = upload(&r->fac32, fac.data(), (size_t)A);
+    if (!rc) rc = upload(&r->W1_32, w1.data(), (size_t)A);
+    if (!rc) rc = upload(&r->W2_32, w2.data(), (size_t)A);
+    if (rc) return rc;
+    const size_t nAC = (size_t)A * nc;
+    if (cudaMalloc((void **)&r->recA, nAC * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc((void **)&r->recB, nAC * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc((void **)&r->PsiM32, (size_t)nLevels * nc * ngr * sizeof(float)) != cudaSuccess)
+      return set_error(UMT_ERR_NOMEM, "RZ: FP32 record allocation failed");
+    const size_t nAZ = (size_t)A * nz;
+    k_rz_prep32<<<(unsigned)((nAZ + 255) / 256), 256>>>(A, nz, nc, c.numCorner, c.cOffSet, r->cEZ2, c.afp64, c.aez64,
+                                                         r->Area, r->RadiusFP, r->RadiusEZ, r->angDerivFac, r->recA,
+                                                         r->recB);
+    UMT_CUDA(cudaGetLastError());
+    UMT_CUDA(cudaDeviceSynchronize());
+  }
   return 0;
 }
 
-int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double *PsiB_inout) {
+// FP32: conversions, stages and tally replayed from one CUDA graph per
+// buffer parity (captured again when tau, a kernel argument, changes);
+// PsiB crosses the host link in FP64 through the context's staging buffer.
+static int sweep_rz32(Ctx &c, RZData &r, int savePsi, double *PhiTotal, double *PsiB_inout) {
+  const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  if (PsiB_inout) {
+    double *tmp = nullptr;
+    TRY_RC(staging_buffer64(c, psiBN, &tmp));
+    UMT_CUDA(cudaMemcpyAsync(tmp, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
+    k_rz_to_float<<<4096, 256, 0, c.stream>>>(psiBN, tmp, c.psiB32);
+  }
+  if (r.graphTau != c.tau) {
+    destroy_rz_graphs(r);
+    r.graphTau = c.tau;
+  }
+  cudaGraphExec_t &ex = r.graph32[c.cur32];
+  if (!ex) {
+    cudaGraph_t gr = nullptr;
+    UMT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_sweep_rz32(c, r);
+    const cudaError_t e = cudaStreamEndCapture(c.stream, &gr);
+    if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+    if (e != cudaSuccess) return set_error(UMT_ERR_CUDA, "RZ graph capture: %s", cudaGetErrorString(e));
+    const cudaError_t ei = cudaGraphInstantiate(&ex, gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess) { ex = nullptr; return set_error(UMT_ERR_CUDA, "RZ graph instantiate: %s", cudaGetErrorString(ei)); }
+  }
+  UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
+  UMT_CUDA(cudaGraphLaunch(ex, c.stream));
+  UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
+  if (PhiTotal) UMT_CUDA(cudaMemcpyAsync(PhiTotal, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (PsiB_inout) {
+    double *tmp = nullptr;
+    TRY_RC(staging_buffer64(c, psiBN, &tmp));
+    k_rz_to_double<<<4096, 256, 0, c.stream>>>(psiBN, c.psiB32, tmp);
+    UMT_CUDA(cudaMemcpyAsync(PsiB_inout, tmp, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
+  }
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  cudaEventElapsedTime(&c.lastMs, c.ev0, c.ev1);
+  if (savePsi) c.cur32 = 1 - c.cur32;
+  return 0;
+}
+
+int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double *PsiB_inout, int precision) {
   Ctx &c = cur();
   if (!c.ready || !c.rz) return set_error(UMT_ERR_STATE, "umt103_init_rz not called");
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
+  if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated (init flags)");
+  if (precision == UMT_FP32 && (!c.psi32[0] || !c.rz->recA)) return set_error(UMT_ERR_STATE, "FP32 flux not allocated (init flags)");
   RZData &r = *c.rz;
   const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
   else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
+  if (precision == UMT_FP32) return sweep_rz32(c, r, savePsi, PhiTotal, PsiB_inout);
   if (PsiB_inout) UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
   UMT_CUDA(cudaMemsetAsync(r.PsiM, 0, (size_t)r.nLevels * ncG * 8, c.stream));
   RZP p;
@@ -428,6 +784,7 @@ int umt103_sweep_rz(const double *STotal, int savePsi, double *PhiTotal, double 
   const int TEAMS = RZ_NT / GT;
   UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
   for (int s = 0; s < r.nStages; ++s) {
+    if (r.hCount[s] == 0) continue;
     p.stageBegin = r.hOffset[s];
     p.stageCount = r.hCount[s];
     const int blocks = (r.hCount[s] + TEAMS - 1) / TEAMS;

@@ -1,6 +1,7 @@
 // sweep32_util.cuh -- device helpers shared by the FP32 sweep kernels
-// (sweep32.cu, sweep32p.cu): team lane masks, asynchronous global->shared
-// copies, and group-pair (float2) loads and stores for the paired FP32
+// (sweep32.cu, sweep32p.cu, rz.cu): team lane masks, asynchronous
+// global->shared copies, programmatic dependent launch, the approximate
+// reciprocal, and group-pair (float2) loads and stores for the paired FP32
 // instructions (FFMA2/FMUL2/FADD2) of sm_100-class GPUs.
 #pragma once
 #include <cuda_runtime.h>
@@ -41,6 +42,14 @@ __device__ __forceinline__ void pdl_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// 1/x for positive, normal x: the hardware reciprocal approximation
+// (rcp.approx.ftz.f32, max. 1 ulp).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 template <int NP>
 __device__ __forceinline__ void ld2(const float *p, float2 (&v)[NP]) {

@@ -71,12 +71,7 @@ __device__ __forceinline__ void ldg2(const float *p, float2 (&v)[NP]) {
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
 // a / b for positive, normal b: the hardware reciprocal approximation
-// (rcp.approx.ftz.f32, max. 1 ulp) times a, one paired multiply per group pair.
-__device__ __forceinline__ float rcp_approx(float x) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
+// (rcp_approx) times a, one paired multiply per group pair.
 __device__ __forceinline__ float2 div2(float2 a, float2 b) {
   return __fmul2_rn(a, make_float2(rcp_approx(b.x), rcp_approx(b.y)));
 }

@@ -158,6 +158,8 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL);
 void default_tile(int G, int *GT, int *GPL);
 // 2-D RZ sweep (rz.cu)
 void free_rz(Ctx &c);
+// persistent FP64 staging buffer of at least n elements (capi.cu)
+int staging_buffer64(Ctx &c, size_t n, double **out);
 // zone-program FP32 kernel (sweep32p.cu)
 int prepare_prog32(Ctx &c);
 bool sweep32p_supported(int G, int GT, int GPL);
