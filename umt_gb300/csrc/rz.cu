@@ -36,7 +36,7 @@ struct RZData {
   int *cFP2 = nullptr, *cEZ2 = nullptr;                              // [nc*2], 0-based
   double *PsiM = nullptr;                                            // [nLevels][nc][G]
   uint32_t *items = nullptr;                                         // stage order, a*nz + z
-  int nLevels = 0, nStages = 0, maxStageItems = 0;
+  int nLevels = 0, nStages = 0, maxStageItems = 0, maxC = 0;
   std::vector<int> hCount, hOffset;
   std::vector<double> hArea, hVolume, hRfp, hRez;
   // FP32 path (init flag bit 1)
@@ -340,22 +340,28 @@ struct RZP32 {
 };
 
 // One dependency stage of the FP32 RZ sweep: a team of GT lanes per
-// (direction, zone), lanes over groups; the operations of k_sweep_rz in the
-// same order, with the EZ closure of a corner face whose FP face is incoming
-// divided through by aez^4 (x = sigma*Area/aez):
-//   sez = RadiusEZ*Area (N (sigma psi_fp - Q_c) + D (Q_c - Q_z)) / (N + 2 x D),
-//   N = 1.82 x^2 + 4 x + 3,  D = 2 x^3 + 3 x^2 + 2 x + 1,
-// algebraically the reference's gnum/gden form; x is capped at 1e8 so every
-// term stays finite in FP32.  Divisions are approximate reciprocals times a
-// multiply.  Programmatic dependent launch: everything before pdl_wait()
-// reads only data no stage writes.
-template <int GT>
-__global__ void __launch_bounds__(RZ_NT) k_sweep_rz32(RZP32 p) {
+// (direction, zone), lanes over groups; MAXC (4 or 8) bounds the corners of
+// a zone, and the corner loops are unrolled to it.  The operations of
+// k_sweep_rz, with three changes of rounding order:
+// * the angular-derivative term Area*angDerivFac*PsiM enters the corner's
+//   source before the solve instead of at it;
+// * the EZ closure of a corner face whose FP face is incoming is divided
+//   through by aez^4 (x = sigma*Area/aez):
+//     sez = RadiusEZ*Area (N (sigma psi_fp - Q_c) + D (Q_c - Q_z)) / (N + 2 x D),
+//     N = 1.82 x^2 + 4 x + 3,  D = 2 x^3 + 3 x^2 + 2 x + 1,
+//   algebraically the reference's gnum/gden form (x is capped at 1e8 so every
+//   term stays finite in FP32);
+// * divisions are approximate reciprocals times a multiply.
+// Offsets within one direction are 32-bit (ncornr*G, nbelem*G and nzones*G
+// are below 2^31, checked at init).  Programmatic dependent launch: everything
+// before pdl_wait() reads only data no stage writes.
+template <int GT, int MAXC>
+__global__ void __launch_bounds__(RZ_NT, MAXC == 4 ? 5 : 4) k_sweep_rz32(RZP32 p) {
   pdl_launch_dependents();
   constexpr int TEAMS = RZ_NT / GT;
-  __shared__ float s_src[RZ_MAXC][RZ_NT], s_Q[RZ_MAXC][RZ_NT], s_pm[RZ_MAXC][RZ_NT];
-  __shared__ float4 s_A[TEAMS][RZ_MAXC], s_B[TEAMS][RZ_MAXC], s_C[TEAMS][RZ_MAXC];
-  __shared__ int2 s_L[TEAMS][RZ_MAXC];
+  __shared__ float s_src[MAXC][RZ_NT], s_Q[MAXC][RZ_NT];
+  __shared__ float4 s_A[TEAMS][MAXC], s_B[TEAMS][MAXC], s_C[TEAMS][MAXC];
+  __shared__ int2 s_L[TEAMS][MAXC];
   const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
   const int k = blockIdx.x * TEAMS + team;
   if (k >= p.stageCount) return;                       // whole teams leave together
@@ -365,7 +371,8 @@ __global__ void __launch_bounds__(RZ_NT) k_sweep_rz32(RZP32 p) {
   const int z = (int)(it - (uint32_t)a * p.nz);
   const int nC = p.numCorner[z], c0 = p.cOffSet[z];
   const uint32_t ord = p.order[it];
-  const size_t abase = (size_t)a * p.nc;
+  const int G = p.G, nc = p.nc;
+  const size_t abase = (size_t)a * nc;
   for (int c = lane; c < nC; c += GT) {
     s_A[team][c] = p.recA[abase + c0 + c];
     s_B[team][c] = p.recB[abase + c0 + c];
@@ -374,52 +381,58 @@ __global__ void __launch_bounds__(RZ_NT) k_sweep_rz32(RZP32 p) {
   }
   const float fac = p.fac[a], W1 = p.W1[a], W2 = p.W2[a];
   const bool start = p.starting[a] != 0, nextFin = p.nextFinishing[a] != 0;
-  float *psiM = p.PsiM + (size_t)p.level[a] * p.nc * p.G;
+  const float *pold = p.psi_old + abase * G;                      // direction a
+  float *pnew = p.psi_new + abase * G;
+  float *pnext = pnew + (size_t)nc * G;                           // direction a + 1
+  float *pB = p.psiB + (size_t)a * p.nb * G;
+  float *pBnext = pB + (size_t)p.nb * G;
+  float *psiM = p.PsiM + (size_t)p.level[a] * nc * G;
+  const int e0 = c0 * G;
   __syncwarp(teammask);
-  pdl_wait();
-  for (int g = lane; g < p.G; g += GT) {
-    const float sig = p.Sigt[(size_t)z * p.G + g];
-    float po[RZ_MAXC], st[RZ_MAXC], pu[RZ_MAXC][2];
+  for (int g = lane; g < G; g += GT) {
+    const float sig = p.Sigt[z * G + g];
 #pragma unroll
-    for (int c = 0; c < RZ_MAXC; ++c) {
-      po[c] = st[c] = pu[c][0] = pu[c][1] = 0.f;
+    for (int c = 0; c < MAXC; ++c)
       if (c < nC) {
-        const size_t e = ((size_t)c0 + c) * p.G + g;
-        po[c] = p.psi_old[abase * p.G + e];
-        st[c] = p.STotal[e];
-        s_pm[c][tid] = psiM[e];
+        const float q = fmaf(p.tau, pold[e0 + c * G + g], p.STotal[e0 + c * G + g]);
+        s_Q[c][tid] = q;
+        s_src[c][tid] = s_C[team][c].x * q;
+      }
+    pdl_wait();                                          // the previous stage is complete from here on
+    float pm[MAXC], pu[MAXC][2];
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {
+      pm[c] = pu[c][0] = pu[c][1] = 0.f;
+      if (c < nC) {
+        pm[c] = psiM[e0 + c * G + g];
         const unsigned bits = __float_as_uint(s_B[team][c].w);
         const int2 L = s_L[team][c];
 #pragma unroll
         for (int f = 0; f < 2; ++f)
           if (bits & (1u << f)) {
             const int cfp = (f ? L.y : L.x) >> 3;
-            pu[c][f] = cfp < p.nc ? p.psi_new[(abase + cfp) * p.G + g]
-                                  : p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g];
+            pu[c][f] = cfp < nc ? pnew[cfp * G + g] : pB[(cfp - nc) * G + g];
           }
       }
     }
     const float rsig = rcp_approx(sig);
+    // corner c's source, kept in a register while its faces are added; other
+    // corners' EZ terms reach it through shared memory (cez != c)
 #pragma unroll
-    for (int c = 0; c < RZ_MAXC; ++c)
-      if (c < nC) {
-        const float q = fmaf(p.tau, po[c], st[c]);
-        s_Q[c][tid] = q;
-        s_src[c][tid] = s_C[team][c].x * q;
-      }
-#pragma unroll
-    for (int c = 0; c < RZ_MAXC; ++c) {
+    for (int c = 0; c < MAXC; ++c) {
       if (c >= nC) continue;
       const float4 A = s_A[team][c], B = s_B[team][c], C = s_C[team][c];
       const unsigned bits = __float_as_uint(B.w);
       const int2 L = s_L[team][c];
+      const float Qc = s_Q[c][tid];
+      float sc = fmaf(C.w * fac, pm[c], s_src[c][tid]);
 #pragma unroll
       for (int f = 0; f < 2; ++f) {
         const float kfp = f ? A.y : A.x, rae = f ? A.w : A.z, xa = f ? B.z : B.y, rza = f ? C.z : C.y;
-        if (bits & (1u << f)) s_src[c][tid] = fmaf(-kfp, pu[c][f], s_src[c][tid]);
+        if (bits & (1u << f)) sc = fmaf(-kfp, pu[c][f], sc);
         if (bits & (16u << f)) {
-          const int cez = (f ? L.y : L.x) & 7;
-          const float Qc = s_Q[c][tid], Qz = s_Q[cez][tid];
+          const int cez = (f ? L.y : L.x) & (MAXC - 1);
+          const float Qz = s_Q[cez][tid];
           float sez;
           if (bits & (1u << f)) {
             const float x = fminf(sig * xa, 1e8f);
@@ -429,42 +442,42 @@ __global__ void __launch_bounds__(RZ_NT) k_sweep_rz32(RZP32 p) {
           } else {
             sez = 0.5f * rae * (Qc - Qz) * rsig;
           }
-          s_src[c][tid] += sez;
+          sc += sez;
           s_src[cez][tid] -= sez;
         }
       }
+      s_src[c][tid] = sc;
     }
-    float *out = p.psi_new + abase * p.G;
 #pragma unroll
-    for (int i = 0; i < RZ_MAXC; ++i) {
+    for (int i = 0; i < MAXC; ++i) {
       if (i >= nC) continue;
-      const int c = (int)((ord >> (4 * i)) & 15u);
+      const int c = (int)((ord >> (4 * i)) & (unsigned)(MAXC - 1));
       const float4 B = s_B[team][c], C = s_C[team][c], A = s_A[team][c];
       const int2 L = s_L[team][c];
-      const float v = fmaf(C.w * fac, s_pm[c][tid], s_src[c][tid]) * rcp_approx(fmaf(sig, C.x, B.x));
-      out[((size_t)c0 + c) * p.G + g] = v;
+      const float v = s_src[c][tid] * rcp_approx(fmaf(sig, C.x, B.x));
+      pnew[e0 + c * G + g] = v;
       s_Q[c][tid] = v;                       // Q is no longer needed: keep the solved flux
       const unsigned bits = __float_as_uint(B.w);
-      if (bits & 16u) s_src[L.x & 7][tid] = fmaf(A.z, v, s_src[L.x & 7][tid]);
-      if (bits & 32u) s_src[L.y & 7][tid] = fmaf(A.w, v, s_src[L.y & 7][tid]);
+      if (bits & 16u) s_src[L.x & (MAXC - 1)][tid] = fmaf(A.z, v, s_src[L.x & (MAXC - 1)][tid]);
+      if (bits & 32u) s_src[L.y & (MAXC - 1)][tid] = fmaf(A.w, v, s_src[L.y & (MAXC - 1)][tid]);
     }
 #pragma unroll
-    for (int c = 0; c < RZ_MAXC; ++c) {
+    for (int c = 0; c < MAXC; ++c) {
       if (c >= nC) continue;
-      const size_t e = ((size_t)c0 + c) * p.G + g;
+      const int e = e0 + c * G + g;
       const float v = s_Q[c][tid];
-      const float m = start ? v : fmaf(W1, v, -W2 * s_pm[c][tid]);
+      const float m = start ? v : fmaf(W1, v, -W2 * pm[c]);
       psiM[e] = m;
-      if (nextFin) p.psi_new[(abase + p.nc) * p.G + e] = m;
+      if (nextFin) pnext[e] = m;
       const unsigned bits = __float_as_uint(s_B[team][c].w);
       const int2 L = s_L[team][c];
 #pragma unroll
       for (int f = 0; f < 2; ++f) {
         const int cfp = (f ? L.y : L.x) >> 3;
-        if ((bits & (4u << f)) && cfp >= p.nc) {
-          const size_t b = (size_t)(cfp - p.nc);
-          p.psiB[((size_t)a * p.nb + b) * p.G + g] = v;
-          if (nextFin) p.psiB[((size_t)(a + 1) * p.nb + b) * p.G + g] = m;
+        if ((bits & (4u << f)) && cfp >= nc) {
+          const int b = (cfp - nc) * G + g;
+          pB[b] = v;
+          if (nextFin) pBnext[b] = m;
         }
       }
     }
@@ -492,14 +505,13 @@ static int enqueue_sweep_rz32(Ctx &c, RZData &r) {
   while (GT < c.G && GT < 32) GT *= 2;
   const int TEAMS = RZ_NT / GT;
   void (*kern)(RZP32) = nullptr;
+#define UMT_RZ32(gt)                                                    \
+  case gt: kern = r.maxC <= 4 ? k_sweep_rz32<gt, 4> : k_sweep_rz32<gt, 8>; break;
   switch (GT) {
-    case 1: kern = k_sweep_rz32<1>; break;
-    case 2: kern = k_sweep_rz32<2>; break;
-    case 4: kern = k_sweep_rz32<4>; break;
-    case 8: kern = k_sweep_rz32<8>; break;
-    case 16: kern = k_sweep_rz32<16>; break;
-    default: kern = k_sweep_rz32<32>; break;
+    UMT_RZ32(1) UMT_RZ32(2) UMT_RZ32(4) UMT_RZ32(8) UMT_RZ32(16)
+    default: kern = r.maxC <= 4 ? k_sweep_rz32<32, 4> : k_sweep_rz32<32, 8>; break;
   }
+#undef UMT_RZ32
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
@@ -591,10 +603,13 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
   for (int a = 0; a < A; ++a) { om3[3 * a] = q->omega[2 * a]; om3[3 * a + 1] = q->omega[2 * a + 1]; }
   UmtQuad q3 = {A, om3.data(), q->weight};
   const int precFlags = (flags & 3) ? (flags & 3) : 3;     // bit 0: FP64 flux, bit 1: FP32 flux
-  if ((precFlags & 2) && (long long)nc + nb >= (1LL << 28)) {
+  if ((precFlags & 2) && ((long long)nc + nb >= (1LL << 28) || (long long)(nc + nb) * ngr >= (1LL << 31) ||
+                          (long long)nz * ngr >= (1LL << 31))) {
     delete r;
-    return set_error(UMT_ERR_ARG, "RZ FP32 path: ncornr + nbelem must be below 2^28");
+    return set_error(UMT_ERR_ARG, "RZ FP32 path: ncornr + nbelem must be below 2^28 and (ncornr + nbelem)*G, "
+                                  "nzones*G below 2^31");
   }
+  for (int zn = 0; zn < nz; ++zn) r->maxC = std::max(r->maxC, m->numCorner[zn]);
   release_current_context();
   Ctx &c = cur();
   int rc = init_context(c, &m3, &q3, ngr, precFlags);
