@@ -248,17 +248,27 @@ def run_rz(args):
     lib.init_rz(m, q, G, flags=2 if prec == capi.UMT_FP32 else 1)
     lib.set_materials(sigt, np.zeros_like(sigt), 1.0 / (299.792458 * 1e-3))
     lib.set_psi(np.full((A, m.ncornr, G), 0.5 / np.pi), None)
-    PsiB = np.zeros((A, m.nbelem, G))
+    # inputs and results in page-locked host memory, allocated once
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    STotal_h = pinned((m.ncornr, G))
+    STotal_h[...] = STotal
+    STotal = STotal_h
+    PsiB = pinned((A, m.nbelem, G))
+    PsiB[...] = 0.0
+    Phi = pinned((m.ncornr, G))
     units = m.ncornr * A * G
     for _ in range(args.warmup):
-        lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB, precision=prec)
+        lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB, precision=prec, Phi=Phi)
     torch.cuda.synchronize()
-    ms, t0 = [], time.perf_counter()
+    ms = []
     with ClockSampler(0) as clk:
+        t0 = time.perf_counter()                # the sampler's start and stop stay outside the window
         for _ in range(args.steps):
-            lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB, precision=prec)
+            lib.sweep_rz(STotal, savePsi=False, PsiB=PsiB, precision=prec, Phi=Phi)
             ms.append(lib.last_ms())
-    t_e2e = (time.perf_counter() - t0) / args.steps
+        t_e2e = (time.perf_counter() - t0) / args.steps
     t_dev = sum(ms) / len(ms)
     line = {"metric": METRIC + " (RZ)", "value": t_dev * 1e6 / units, "unit": "ns", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev, "higher_is_better": False,
@@ -269,7 +279,8 @@ def run_rz(args):
                        "units_per_step": units, "psi": args.precision, "tallies": "fp64",
                        "l2": "angular flux %.2f GB per buffer" % (units * (4 if prec == capi.UMT_FP32 else 8) / 1e9)},
             "e2e": {"value": t_e2e * 1e9 / units, "unit": "ns",
-                    "h2d_bytes_per_step": STotal.nbytes + PsiB.nbytes, "d2h_bytes_per_step": STotal.nbytes + PsiB.nbytes},
+                    "h2d_bytes_per_step": STotal.nbytes + PsiB.nbytes, "d2h_bytes_per_step": Phi.nbytes + PsiB.nbytes,
+                    "host_memory": "pinned"},
             "clocks": clk.summary()}
     if not args.no_cpu_baseline:
         from oracle import pyoracle as po

@@ -97,6 +97,37 @@ def test_rz_fp32_sweep_matches_oracle(umtlib, nr, nzr, P, Az, G, index_base):
     assert rel_err(PB, PsiB_ref) < FP32_PSI_TOL
 
 
+@pytest.mark.parametrize("precision", [capi.UMT_FP64, capi.UMT_FP32])
+def test_rz_mixed_polygons_match_oracle(umtlib, precision):
+    """Triangles, quadrilaterals and hexagons in one mesh (the FP32 kernel's
+    8-corner instantiation and 3-corner zones)."""
+    from umt_gb300.mesh_rz import build_rz_mixed_mesh
+    m = build_rz_mixed_mesh(7, 6, distort=0.15, seed=5)
+    assert set(np.unique(m.numCorner)) == {3, 4, 6}
+    q = product_quadrature_rz(2, 3)
+    G = 8
+    rng = np.random.default_rng(9)
+    sigt = rng.uniform(0.2, 20.0, size=(m.nzones, G))
+    STotal = rng.uniform(0.05, 1.0, size=(m.ncornr, G))
+    psi0 = rng.uniform(0.01, 0.2, size=(len(q.weight), m.ncornr, G))
+    PsiB = rng.uniform(0.0, 0.05, size=(len(q.weight), m.nbelem, G))
+    tau = 0.4
+    geo, Phi_ref, Psi_ref, PsiB_ref = _oracle(m, q, sigt, STotal, psi0, PsiB, tau)
+    umtlib.init_rz(m, q, G)
+    g = umtlib.geometry_rz()
+    for k in ("Area", "Volume", "RadiusFP", "RadiusEZ"):
+        assert np.array_equal(g[k], geo[k]), k
+    umtlib.set_materials(sigt, np.zeros_like(sigt), tau)
+    umtlib.set_psi(psi0, None)
+    PB = PsiB.copy()
+    Phi = umtlib.sweep_rz(STotal, savePsi=True, PsiB=PB, precision=precision)
+    Psi, _ = umtlib.get_psi(precision)
+    tol_phi, tol_psi = (1e-12, 1e-12) if precision == capi.UMT_FP64 else (FP32_PHI_TOL, FP32_PSI_TOL)
+    assert rel_err(Phi, Phi_ref) < tol_phi
+    assert rel_err(Psi, Psi_ref) < tol_psi
+    assert rel_err(PB, PsiB_ref) < tol_psi
+
+
 def test_rz_fp32_repeated_sweeps_and_tau_change(umtlib):
     """FP32 sweeps replayed from graphs of both buffer parities, and captured
     again after tau changes, stay within the FP32 tolerance of the oracle."""

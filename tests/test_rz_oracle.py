@@ -36,6 +36,42 @@ def test_rz_geometry_invariants(distort):
     assert (geo["A_fp"][..., 2] == 0).all() and (geo["A_ez"][..., 2] == 0).all()
 
 
+def test_rz_polygon_builder_reproduces_the_grid():
+    from umt_gb300.mesh_rz import build_rz_polygon_mesh, _grid
+    m = build_rz_mesh(4, 3, distort=0.1, seed=3)
+    R, Z = _grid(4, 3, 0.2, 1.2, 0.0, 1.0, 0.1, 3)
+    vix = lambda i, j: i * 4 + j
+    polys = [[vix(i, j), vix(i + 1, j), vix(i + 1, j + 1), vix(i, j + 1)] for i in range(4) for j in range(3)]
+    m2 = build_rz_polygon_mesh(np.stack([R.ravel(), Z.ravel()], 1), polys)
+    for k in ("numCorner", "cOffSet", "zoneFaces", "zoneOpp", "faceOpp", "cFP", "cEZ", "CToFace", "px", "bdyToC"):
+        assert np.array_equal(getattr(m, k), getattr(m2, k)), k
+
+
+def test_rz_mixed_mesh_geometry():
+    """Triangles, quadrilaterals and hexagons: corner areas close to the zone's
+    shoelace area, shared faces are exact negations, every zone closes."""
+    from umt_gb300.mesh_rz import build_rz_mixed_mesh
+    m = build_rz_mixed_mesh(6, 5, distort=0.15, seed=7)
+    assert set(np.unique(m.numCorner)) == {3, 4, 6}
+    geo = po.geometry_rz(m)
+    for z in range(m.nzones):
+        c0, n = m.cOffSet[z], m.numCorner[z]
+        p = m.px[c0:c0 + n]
+        shoelace = 0.5 * (np.dot(p[:, 0], np.roll(p[:, 1], -1)) - np.dot(p[:, 1], np.roll(p[:, 0], -1)))
+        assert shoelace > 0
+        assert abs(geo["Area"][c0:c0 + n].sum() - shoelace) < 1e-14
+        assert abs(geo["A_fp"][c0:c0 + n].sum(axis=(0, 1))).max() < 1e-15
+    for c in range(m.ncornr):
+        for f in range(2):
+            v = m.cFP[c, f]
+            if v < m.ncornr:
+                assert np.array_equal(geo["A_fp"][c, f], -geo["A_fp"][v, 1 - f])
+                assert np.array_equal(m.px[v], m.px[c])
+    with pytest.raises(ValueError):
+        from umt_gb300.mesh_rz import build_rz_polygon_mesh
+        build_rz_polygon_mesh(np.array([[0.2, 0.0], [1.0, 0.0], [0.2, 1.0]]), [[0, 2, 1]])   # clockwise
+
+
 @pytest.mark.parametrize("P,Az", [(1, 1), (2, 2), (4, 4), (8, 6)])
 def test_rz_quadrature(P, Az):
     q = product_quadrature_rz(P, Az)

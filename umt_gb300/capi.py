@@ -330,10 +330,14 @@ class Library:
         self.A, self.G, self.nz, self.nc, self.nb = len(q.weight), int(ngr), m.nzones, m.ncornr, m.nbelem
         return self
 
-    def sweep_rz(self, STotal=None, savePsi=False, PsiB=None, precision=UMT_FP64):
-        """umt103_sweep_rz; returns PhiTotal, PsiB is updated in place."""
+    def sweep_rz(self, STotal=None, savePsi=False, PsiB=None, precision=UMT_FP64, Phi=None):
+        """umt103_sweep_rz; returns PhiTotal (written into Phi when given, a
+        C-contiguous float64 (nc, G) array), PsiB is updated in place."""
         STotal = _c(STotal, np.float64)
-        Phi = np.zeros((self.nc, self.G))
+        if Phi is not None:
+            assert Phi.dtype == np.float64 and Phi.flags.c_contiguous and Phi.shape == (self.nc, self.G)
+        else:
+            Phi = np.zeros((self.nc, self.G))
         if PsiB is not None:
             assert PsiB.dtype == np.float64 and PsiB.flags.c_contiguous
         check(self.lib.umt103_sweep_rz(_d(STotal), int(bool(savePsi)), _d(Phi), _d(PsiB), int(precision)))

@@ -198,29 +198,51 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
 
 // psi -> phi tally: PhiTotal(g,c) = sum_a w_a psi_a(g,c), accumulated in FP64
 // (control/getPhiTotal_OMPOL.F90:63-131 does the same per direction).
-// FP32 angular flux: each thread owns 4 consecutive (corner, group) entries;
-// products w_a*psi_a of one block of 8 directions are summed in FP32 and the
-// block sums are accumulated in FP64.  GB300's FP64 rate is 1/64 of FP32, so
-// an FP64 multiply-add per (direction, entry) would make this HBM pass
-// FP64-bound; one FP64 add per 8 directions keeps it at the read bandwidth.
-__global__ void __launch_bounds__(256) k_tally32(int A, size_t ncG, const float *w32, const float *psi, double *Phi) {
+// FP32 angular flux: each thread owns 4 consecutive (corner, group) entries
+// and sums w_a*psi_a over the directions with compensated (Kahan) FP32
+// summation, the product entering each step unrounded; the sum and its
+// compensation are combined in FP64 at the end.  The error is a few FP32 ulps
+// of the sum whatever the number of directions, and the loop holds no FP64
+// operation: GB300's FP64 rate is 1/64 of FP32, and FP64 accumulation kept
+// the FP64 pipe ~60% busy and this pass below the read bandwidth.  Each
+// thread has 16 float4 loads in flight.
+__device__ __forceinline__ void kahan_add(float &s, float &c, float w, float x) {
+  const float y = fmaf(w, x, -c);           // the product enters unrounded
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+__global__ void __launch_bounds__(256) k_tally32(int A, size_t ncG, const float *__restrict__ w32,
+                                                 const float *__restrict__ psi, double *__restrict__ Phi) {
+  constexpr int U = 16;                       // float4 loads in flight per thread
   const size_t n4 = ncG / 4;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n4; q += (size_t)gridDim.x * blockDim.x) {
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int a0 = 0; a0 < A; a0 += 8) {
-      float s[4] = {0.f, 0.f, 0.f, 0.f};
-      const int a1 = min(A, a0 + 8);
-#pragma unroll 8
-      for (int a = a0; a < a1; ++a) {
-        const float w = w32[a];
-        const float4 v = *reinterpret_cast<const float4 *>(psi + (size_t)a * ncG + 4 * q);
-        s[0] = fmaf(w, v.x, s[0]); s[1] = fmaf(w, v.y, s[1]); s[2] = fmaf(w, v.z, s[2]); s[3] = fmaf(w, v.w, s[3]);
-      }
+    float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
+    const float *p = psi + 4 * q;
+    int a = 0;
+    for (; a + U <= A; a += U) {
+      float4 v[U];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[j] += (double)s[j];
+      for (int u = 0; u < U; ++u) v[u] = *reinterpret_cast<const float4 *>(p + (size_t)(a + u) * ncG);
+      asm volatile("" ::: "memory");          // issue all U loads before the first sum
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const float w = w32[a + u];
+        kahan_add(s[0], c[0], w, v[u].x); kahan_add(s[1], c[1], w, v[u].y);
+        kahan_add(s[2], c[2], w, v[u].z); kahan_add(s[3], c[3], w, v[u].w);
+      }
     }
-    *reinterpret_cast<double2 *>(Phi + 4 * q) = make_double2(acc[0], acc[1]);
-    *reinterpret_cast<double2 *>(Phi + 4 * q + 2) = make_double2(acc[2], acc[3]);
+    for (; a < A; ++a) {
+      const float w = w32[a];
+      const float4 v = *reinterpret_cast<const float4 *>(p + (size_t)a * ncG);
+      kahan_add(s[0], c[0], w, v.x); kahan_add(s[1], c[1], w, v.y);
+      kahan_add(s[2], c[2], w, v.z); kahan_add(s[3], c[3], w, v.w);
+    }
+    *reinterpret_cast<double2 *>(Phi + 4 * q) =
+        make_double2((double)s[0] - (double)c[0], (double)s[1] - (double)c[1]);
+    *reinterpret_cast<double2 *>(Phi + 4 * q + 2) =
+        make_double2((double)s[2] - (double)c[2], (double)s[3] - (double)c[3]);
   }
   for (size_t e = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncG; e += (size_t)gridDim.x * blockDim.x) {
     double t = 0.0;
