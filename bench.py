@@ -395,8 +395,15 @@ def main():
         tt = torch.tensor([t_e2e], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
-    h2d = STotal.nbytes + PsiB.nbytes
-    d2h = Phi.nbytes + PsiB.nbytes
+    if prec == capi.UMT_FP32:
+        # the FP32 call moves the PsiB rows the sweep reads in and the rows it writes out
+        ex_rows, all_rows = lib.psib_rows()
+        row_bytes = G * 8
+        h2d = STotal.nbytes + (all_rows - ex_rows) * row_bytes
+        d2h = Phi.nbytes + ex_rows * row_bytes
+    else:
+        h2d = STotal.nbytes + PsiB.nbytes
+        d2h = Phi.nbytes + PsiB.nbytes
 
     if rank != 0:
         if dist:
@@ -426,7 +433,10 @@ def main():
                      "bytes_per_unit": balg, "kernel_ms": k_avg, "tally_ms": sum(tally_ms) / len(tally_ms)},
         "e2e": {"value": t_e2e * 1e9 / (units * world), "unit": "ns", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "host_memory": "pinned",
-                "call": "umt103_sweep(STotal, savePsi=0, PhiTotal, PsiB inout, FP32)"},
+                "call": "umt103_sweep(STotal, savePsi=0, PhiTotal, PsiB inout, %s)" %
+                        ("FP32" if prec == capi.UMT_FP32 else "FP64"),
+                "psib": ("rows the sweep reads in, rows it writes out (FP64 host array)"
+                         if prec == capi.UMT_FP32 else "whole array both ways")},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
     }

@@ -310,6 +310,14 @@ int umt103_set_sweep_mode(int mode);
 /* Number of kernels one sweep of the given precision launches (>= 0). */
 int umt103_launches_per_sweep(int precision);
 
+/* PsiB rows (direction, boundary element) of the current 3-D context: how
+ * many the FP32 sweep writes (exiting faces) of the A*nbelem in all.  An FP32
+ * umt103_sweep moves only the other rows host -> device and only the
+ * exiting rows device -> host; the caller's PsiB keeps every row the sweep
+ * does not write bit for bit (snac/SweepUCBxyz.F90 writes PsiB only on the
+ * exit list).  No counterpart in the reference. */
+int umt103_psib_rows(long long *exiting, long long *total);
+
 /* Make `device` current for the calling thread before umt103_init (one
  * process per GPU; the reference binds ranks to GPUs the same way). */
 int umt103_select_device(int device);

@@ -158,6 +158,39 @@ def test_batch_of_contexts_matches_single_runs(umtlib):
         umtlib.context_destroy(cid)
 
 
+@pytest.mark.parametrize("pinned", [False, True])
+def test_fp32_sweep_writes_only_exiting_psib_rows(umtlib, pinned):
+    """An FP32 sweep writes the caller's PsiB only on exiting rows, as the
+    reference writes PsiB only on the exit list: every row the oracle leaves
+    unchanged keeps its FP64 input bit for bit, exiting rows agree with the
+    oracle to the FP32 tolerance, and umt103_psib_rows counts them."""
+    prob = synthetic_problem((3, 2, 2), 2, 2, 8, seed=4, time_dependent=True)
+    m = prob.mesh
+    A, G = len(prob.weight), prob.ngr
+    rng = np.random.default_rng(5)
+    PsiB0 = rng.uniform(0.0, 0.1, size=(A, m.nbelem, G))
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    ref = oracle_sweep(prob, savePsi=False, STotal=STotal, Psi=prob.psi0, PsiB=PsiB0)
+    umtlib.init(m, prob.omega, prob.weight, G)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    if pinned:
+        torch = pytest.importorskip("torch")
+        PsiB = torch.empty((A, m.nbelem, G), dtype=torch.float64, pin_memory=True).numpy()
+    else:
+        PsiB = np.empty((A, m.nbelem, G))
+    PsiB[...] = PsiB0
+    Phi = umtlib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=capi.UMT_FP32)
+    kept = np.all(ref["PsiB"] == PsiB0, axis=2)                  # rows the oracle did not write
+    assert kept.any() and (~kept).any()
+    assert np.array_equal(PsiB[kept], PsiB0[kept])
+    assert rel_err(PsiB[~kept], ref["PsiB"][~kept]) < 1e-4
+    assert rel_err(Phi, ref["Phi"]) < 1e-5
+    ex, tot = umtlib.psib_rows()
+    assert tot == A * m.nbelem
+    assert ex == (~kept).sum()                                  # the same exit rows as the oracle's
+
+
 def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):
     """Page-locked and pageable host arrays give bit-identical sweeps, with
     incoming boundary fluxes set and exits returned (the bench passes

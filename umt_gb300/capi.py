@@ -95,7 +95,7 @@ def load():
                   "umt103_set_gta", "umt103_tally_noalloc", "umt103_context_create",
                   "umt103_init_rz", "umt103_sweep_rz", "umt103_get_geometry_rz",
                   "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
-                  "umt103_batch_sweep"):
+                  "umt103_batch_sweep", "umt103_psib_rows"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
@@ -113,7 +113,7 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_set_sweep_mode", "umt103_set_gta", "umt103_tally_noalloc",
             "umt103_context_create", "umt103_context_select", "umt103_context_current",
             "umt103_context_destroy", "umt103_batch_sweep", "umt103_init_rz", "umt103_sweep_rz",
-            "umt103_get_geometry_rz"]
+            "umt103_get_geometry_rz", "umt103_psib_rows"]
 
 
 def check(rc):
@@ -225,6 +225,12 @@ class Library:
         if n < 0:
             check(n)
         return n
+
+    def psib_rows(self):
+        """(exiting, total) PsiB rows of the FP32 sweep (umt103_psib_rows)."""
+        ex, tot = C.c_longlong(0), C.c_longlong(0)
+        check(self.lib.umt103_psib_rows(C.byref(ex), C.byref(tot)))
+        return ex.value, tot.value
 
     def source_iterate(self, precision=UMT_FP64, max_iters=50, rel_tol=1e-8, q_ext=None, save_psi=True,
                        use_gta=False, allow_notconv=False, warm_start=False):

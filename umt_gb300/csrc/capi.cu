@@ -73,7 +73,7 @@ static void free_ctx(Ctx &c) {
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red);
   dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
-  dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64);
+  dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
   c.stage64N = 0;
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
@@ -409,6 +409,65 @@ __global__ void k_f2d(size_t n, const float *x, double *y) {
     y[i] = (double)x[i];
 }
 
+// Boundary element b's corner face c*3 + f (cFP holds nc + b on boundary faces).
+__global__ void k_bface(int nc, int nb, const int *nCFaces, const int *cFP, int *bFace) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int f = 0; f < nCFaces[c]; ++f) {
+    const int v = cFP[c * UMT_MAXCF + f];
+    if (v >= nc && v - nc < nb) bFace[v - nc] = c * UMT_MAXCF + f;
+  }
+}
+
+// PsiB rows (direction a, boundary element b; G values each) as the FP32
+// sweep kernels classify them: a row is exiting when the FP32 projection
+// Omega_a.A_fp of b's corner face is > 0 (the sweep writes it), every other
+// row is left as it is (the sweep reads it when the projection is < 0).
+// out == 0: every non-exiting row, FP64 -> psiB32; out == 1: every exiting
+// row, psiB32 -> FP64.  src/dst may be page-locked host memory.
+__global__ void k_psib_rows(int A, int nb, int nc, int G, const int *bFace, const float *afp32, const double *src,
+                            float *psiB32, double *dst, int out) {
+  const size_t n = (size_t)A * nb * G;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = i / (size_t)G;
+    const int a = (int)(row / (size_t)nb), b = (int)(row - (size_t)a * nb);
+    const int bf = bFace[b];
+    const bool exiting = bf >= 0 && afp32[(size_t)a * nc * UMT_MAXCF + bf] > 0.f;
+    if (out == 0 && !exiting) psiB32[i] = (float)src[i];
+    if (out == 1 && exiting) dst[i] = (double)psiB32[i];
+  }
+}
+
+__global__ void k_count_exit_rows(int A, int nb, int nc, const int *bFace, const float *afp32,
+                                  unsigned long long *count) {
+  const size_t n = (size_t)A * nb;
+  unsigned long long k = 0;
+  for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < n; r += (size_t)gridDim.x * blockDim.x) {
+    const int a = (int)(r / (size_t)nb), b = (int)(r - (size_t)a * nb);
+    const int bf = bFace[b];
+    k += (bf >= 0 && afp32[(size_t)a * nc * UMT_MAXCF + bf] > 0.f) ? 1 : 0;
+  }
+  if (k) atomicAdd(count, k);
+}
+
+static int ensure_bface(Ctx &c) {
+  if (c.bFace) return 0;
+  TRY(dalloc(&c.bFace, std::max(c.nb, 1)));
+  UMT_CUDA(cudaMemset(c.bFace, 0xff, (size_t)std::max(c.nb, 1) * sizeof(int)));
+  k_bface<<<(c.nc + 255) / 256, 256>>>(c.nc, c.nb, c.nCFaces, c.cFP, c.bFace);
+  UMT_CUDA(cudaGetLastError());
+  UMT_CUDA(cudaDeviceSynchronize());
+  return 0;
+}
+
+// The device address of page-locked host memory, or null for pageable memory.
+static double *mapped_host(double *p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return (double *)at.devicePointer;
+}
+
 int umt103_set_psi(const double *Psi, const double *PsiB) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
@@ -524,14 +583,24 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
   else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
+  // FP32: only the rows a sweep reads go in and only the rows it writes come
+  // out, so the caller's array keeps its other rows bit for bit.  Page-locked
+  // host memory is read and written by the row kernels directly; pageable
+  // memory goes through the FP64 staging buffer, which keeps the input rows.
+  double *psibHost = nullptr, *psibFP64 = nullptr;
   if (PsiB_inout) {
     if (precision == UMT_FP64) {
       UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
     } else {
-      double *tmp = nullptr;
-      TRY(staging64(c, psiBN, &tmp));
-      UMT_CUDA(cudaMemcpyAsync(tmp, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
-      k_d2f<<<4096, 256, 0, c.stream>>>(psiBN, tmp, c.psiB32);
+      TRY(ensure_bface(c));
+      psibHost = mapped_host(PsiB_inout);
+      psibFP64 = psibHost;
+      if (!psibFP64) {
+        TRY(staging64(c, psiBN, &psibFP64));
+        UMT_CUDA(cudaMemcpyAsync(psibFP64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
+      }
+      k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, psibFP64, c.psiB32, nullptr, 0);
+      UMT_CUDA(cudaGetLastError());
     }
   }
   TRY(sweep_core(savePsi, precision));
@@ -540,10 +609,9 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
     if (precision == UMT_FP64) {
       UMT_CUDA(cudaMemcpyAsync(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
     } else {
-      double *tmp = nullptr;
-      TRY(staging64(c, psiBN, &tmp));
-      k_f2d<<<4096, 256, 0, c.stream>>>(psiBN, c.psiB32, tmp);
-      UMT_CUDA(cudaMemcpyAsync(PsiB_inout, tmp, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
+      k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, nullptr, c.psiB32, psibFP64, 1);
+      UMT_CUDA(cudaGetLastError());
+      if (!psibHost) UMT_CUDA(cudaMemcpyAsync(PsiB_inout, psibFP64, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
     }
   }
   UMT_CUDA(cudaStreamSynchronize(c.stream));
@@ -561,6 +629,27 @@ int umt103_last_timing(double *out3) {
 int umt103_launches_per_sweep(int precision) {
   if (precision != 0 && precision != 1) return set_error(UMT_ERR_ARG, "precision");
   return cur().launchesPerSweep[precision];
+}
+
+int umt103_psib_rows(long long *exiting, long long *total) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!exiting || !total) return set_error(UMT_ERR_ARG, "null output");
+  if (!c.afp32) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
+  if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem");
+  TRY(ensure_bface(c));
+  unsigned long long *cnt = nullptr;
+  TRY(dalloc(&cnt, 1));
+  cudaMemset(cnt, 0, sizeof(unsigned long long));
+  k_count_exit_rows<<<1024, 256>>>(c.A, c.nb, c.nc, c.bFace, c.afp32, cnt);
+  unsigned long long h = 0;
+  cudaMemcpy(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(cnt);
+  if (e != cudaSuccess) return set_error(UMT_ERR_CUDA, "psib_rows: %s", cudaGetErrorString(e));
+  *exiting = (long long)h;
+  *total = (long long)c.A * c.nb;
+  return 0;
 }
 
 int umt103_set_gta(int max_krylov, double tol, int spectrum) {

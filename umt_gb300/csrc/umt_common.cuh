@@ -97,6 +97,7 @@ struct Ctx {
   unsigned int *status = nullptr;               // device status word
   double *scratch = nullptr;                    // reductions
   size_t scratchBytes = 0;
+  int *bFace = nullptr;                         // [nb] corner face c*3 + f of each boundary element (-1: none)
   double *stage64 = nullptr;                    // FP64 staging of PsiB for FP32 sweeps (kept)
   size_t stage64N = 0;
   // captured sweep graphs per precision
