@@ -56,9 +56,7 @@ static void free_all() {
 }
 
 static void free_ctx(Ctx &c) {
-  for (int i = 0; i < 2; ++i)
-    for (int j = 0; j < 2; ++j)
-      if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
+  invalidate_graphs(c);
   dfree(c.numCorner); dfree(c.cOffSet); dfree(c.zoneFaces); dfree(c.zoneOpp); dfree(c.faceOpp);
   dfree(c.nCFaces); dfree(c.cFP); dfree(c.cEZ); dfree(c.CToFace); dfree(c.bdyToC); dfree(c.cToZone);
   dfree(c.px); dfree(c.A_fp); dfree(c.A_ez); dfree(c.Volume); dfree(c.VolumeZone); dfree(c.A_bdy);
@@ -74,6 +72,7 @@ static void free_ctx(Ctx &c) {
   dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
+  dfree(c.psibOut);
   c.stage64N = 0;
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
@@ -379,6 +378,7 @@ static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int fla
     TRY(dalloc(&c.Sigt32, nzG)); TRY(dalloc(&c.STotal32, ncG));
     for (int i = 0; i < 2; ++i) { TRY(dalloc(&c.psi32[i], psiN)); UMT_CUDA(cudaMemset(c.psi32[i], 0, psiN * 4)); }
     TRY(dalloc(&c.psiB32, psiBN)); UMT_CUDA(cudaMemset(c.psiB32, 0, psiBN * 4));
+    TRY(dalloc(&c.psibOut, 1)); UMT_CUDA(cudaMemset(c.psibOut, 0, sizeof(double *)));
   }
   UMT_CUDA(cudaDeviceSynchronize());
   c.ready = true;
@@ -459,6 +459,8 @@ static int ensure_bface(Ctx &c) {
   UMT_CUDA(cudaDeviceSynchronize());
   return 0;
 }
+
+__global__ void k_set_word(double **word, double *value) { *word = value; }
 
 // The device address of page-locked host memory, or null for pageable memory.
 static double *mapped_host(double *p) {
@@ -600,16 +602,25 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
         UMT_CUDA(cudaMemcpyAsync(psibFP64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
       }
       k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, psibFP64, c.psiB32, nullptr, 0);
+      // the zone-program kernel writes exiting rows straight to the FP64
+      // destination during the sweep (16-byte stores: needs a 16-byte base)
+      c.wantExitsThrough = ((uintptr_t)psibFP64 & 15u) == 0;
+      k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, c.wantExitsThrough ? psibFP64 : nullptr);
       UMT_CUDA(cudaGetLastError());
     }
   }
-  TRY(sweep_core(savePsi, precision));
+  const int rcs = sweep_core(savePsi, precision);
+  const bool wrote = c.wantExitsThrough && c.exitsThrough;
+  c.wantExitsThrough = false;
+  if (psibFP64) k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, nullptr);   // resident sweeps write nothing
+  TRY(rcs);
   if (PhiTotal_out) UMT_CUDA(cudaMemcpyAsync(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));
   if (PsiB_inout) {
     if (precision == UMT_FP64) {
       UMT_CUDA(cudaMemcpyAsync(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
     } else {
-      k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, nullptr, c.psiB32, psibFP64, 1);
+      if (!wrote)
+        k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, nullptr, c.psiB32, psibFP64, 1);
       UMT_CUDA(cudaGetLastError());
       if (!psibHost) UMT_CUDA(cudaMemcpyAsync(PsiB_inout, psibFP64, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
     }

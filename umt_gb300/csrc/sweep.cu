@@ -324,6 +324,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
   c.launchesPerSweep[prec] = c.sch.nStages + 1 + (sizeof(T) == 4 ? 2 : 0);
   bool done = false;
   if constexpr (sizeof(T) == 4) {
+    c.exitsThrough = false;                   // set again by the zone-program path below
     const size_t n = (size_t)c.nz * c.G;
     k_to_float<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(n, c.Sigt, c.Sigt32);
     const size_t m = (size_t)c.nc * c.G;
@@ -389,6 +390,8 @@ void invalidate_graphs(Ctx &c) {
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j)
       if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
+  for (auto &g : c.graphsWT)
+    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }
 
 // Capture one sweep (source conversion, every dependency stage, tally) for
@@ -396,7 +399,7 @@ void invalidate_graphs(Ctx &c) {
 // sweeps replay it with a single launch.
 static int sweep_via_graph(Ctx &c, int precision) {
   const int cur = precision == 0 ? c.cur64 : c.cur32;
-  cudaGraphExec_t &ex = c.graphs[precision][cur];
+  cudaGraphExec_t &ex = (precision == 1 && c.wantExitsThrough) ? c.graphsWT[cur] : c.graphs[precision][cur];
   if (!ex) {
     cudaGraph_t gr = nullptr;
     UMT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));

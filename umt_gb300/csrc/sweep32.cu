@@ -695,8 +695,10 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   UMT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const int stride4 = 40 * c.G + ((((c.G - (40 * c.G) % 32) % 32) + 32) % 32);
   const size_t smem4 = (size_t)TEAMS * stride4 * sizeof(float);
+  c.exitsThrough = false;
   if (c.sweepMode == 0) {
     const int rc = enqueue_sweep32p(c, cur, GT, GPL);
+    if (rc == 0) c.exitsThrough = true;            // the program kernel writes *psibOut's rows
     if (rc <= 0) return rc;                        // 1: no program kernel for this tile
   }
 #define UMT_LAUNCH4(gt, gpl)                                                                       \

@@ -56,6 +56,7 @@ struct ProgP {
   float tau;
   const float *psi_old;
   float *psi_new, *psiB;
+  double *const *psibOut;               // device word: FP64 copy of the exiting PsiB rows, or null
 };
 
 template <int NP>
@@ -80,7 +81,9 @@ __device__ __forceinline__ float2 div2(float2 a, float2 b) {
 // pair padded to a whole number of 32-bank spans.
 __host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 * 32; }
 
-template <int GT, int GPL>
+// WT: also write the exiting rows, in FP64, to *p.psibOut (the variant used
+// by calls that return PsiB to the host; resident sweeps run the other).
+template <int GT, int GPL, bool WT>
 __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, int stage) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
   constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
@@ -104,6 +107,8 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   unsigned char *sB = reinterpret_cast<unsigned char *>(smem4) + (size_t)TEAMS * p.tstride * 4 +
                       (size_t)team * p.bstride;
   const uint4 h = p.hdr[p.stageOffset[stage] + k];
+  double *hb = nullptr;
+  if constexpr (WT) hb = *p.psibOut;               // read with the header: off the exit path's chain
   const bool bad = (h.x >> 31) != 0;
   const uint32_t it = h.x & 0x7fffffffu;
   const int a = (int)(((unsigned long long)it * p.nzMagic) >> p.nzShift);
@@ -281,11 +286,23 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
     st2<NP>(res + c * RP + g0, v);
     st2<NP>(psiNew + (size_t)(c0 + c) * G, v);
   }
+  // exiting boundary fluxes; with WT the same rows also go, in FP64, to the
+  // caller's PsiB (page-locked host memory) or its staging copy when one is set
+  double *hbA = nullptr;
+  if constexpr (WT) hbA = hb ? hb + (size_t)a * p.nb * G + g0 : nullptr;
   for (int x = 0; x < nX; ++x) {
     const uint32_t e = ex[x];
     float2 v[NP];
     ld2<NP>(res + (int)((e >> 28) & 7u) * RP + g0, v);
-    st2<NP>(psiBA + (size_t)(e & 0x0fffffffu) * G, v);
+    const size_t b = (size_t)(e & 0x0fffffffu);
+    st2<NP>(psiBA + b * G, v);
+    if constexpr (WT) {
+      if (hbA) {
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+          *reinterpret_cast<double2 *>(hbA + b * G + 2 * q) = make_double2((double)v[q].x, (double)v[q].y);
+      }
+    }
   }
 }
 
@@ -652,7 +669,9 @@ int prepare_prog32(Ctx &c) {
   }
   c.progBytes = (size_t)total * 16;
   c.progMaxChunks = (int)hf[1];
-#define UMT_ATTRP(gt, gpl) TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl>));
+#define UMT_ATTRP(gt, gpl)                                                    \
+  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, false>));      \
+  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, true>));
 #define TRY_RC_P(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
   UMT_ATTRP(1, 2) UMT_ATTRP(2, 2) UMT_ATTRP(4, 2) UMT_ATTRP(8, 2) UMT_ATTRP(16, 2) UMT_ATTRP(32, 2)
   UMT_ATTRP(1, 4) UMT_ATTRP(2, 4) UMT_ATTRP(4, 4) UMT_ATTRP(8, 4) UMT_ATTRP(16, 4) UMT_ATTRP(32, 4)
@@ -683,6 +702,7 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
   p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
+  p.psibOut = c.psibOut;
   const int TEAMS = P32_NT / GT;
   const size_t smem = (size_t)TEAMS * ((size_t)p.tstride * 4 + p.bstride);
   // Stage 0 follows the source conversion with ordinary stream order; every
@@ -696,11 +716,13 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   cfg.stream = c.stream;
 #define UMT_LAUNCHP(gt, gpl)                                                                   \
   if (GT == gt && GPL == gpl) {                                                                \
+    void (*kern)(ProgP, int) = c.wantExitsThrough ? k_sweep32p<gt, gpl, true>                  \
+                                                  : k_sweep32p<gt, gpl, false>;                \
     for (int s = 0; s < c.sch.nStages; ++s) {                                                  \
       cfg.gridDim = dim3((c.sch.hCount[s] + TEAMS - 1) / TEAMS);                               \
       cfg.attrs = s > 0 && c.usePDL ? pdl : nullptr;                                           \
       cfg.numAttrs = s > 0 && c.usePDL ? 1 : 0;                                                \
-      UMT_CUDA(cudaLaunchKernelEx(&cfg, k_sweep32p<gt, gpl>, p, s));                           \
+      UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p, s));                                          \
     }                                                                                          \
     return 0;                                                                                  \
   }

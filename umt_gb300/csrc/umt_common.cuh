@@ -98,6 +98,11 @@ struct Ctx {
   double *scratch = nullptr;                    // reductions
   size_t scratchBytes = 0;
   int *bFace = nullptr;                         // [nb] corner face c*3 + f of each boundary element (-1: none)
+  double **psibOut = nullptr;                   // device word read by the zone-program kernel: FP64
+                                                // destination of the exiting PsiB rows, or null
+  bool exitsThrough = false;                    // the FP32 sweep as enqueued runs the zone-program kernel
+  bool wantExitsThrough = false;                // enqueue its variant that writes *psibOut
+  cudaGraphExec_t graphsWT[2] = {nullptr, nullptr};   // FP32 sweeps of that variant, [cur]
   double *stage64 = nullptr;                    // FP64 staging of PsiB for FP32 sweeps (kept)
   size_t stage64N = 0;
   // captured sweep graphs per precision
