@@ -189,6 +189,11 @@ def test_fp32_sweep_writes_only_exiting_psib_rows(umtlib, pinned):
     ex, tot = umtlib.psib_rows()
     assert tot == A * m.nbelem
     assert ex == (~kept).sum()                                  # the same exit rows as the oracle's
+    # the device's FP32 copy (what the energy tallies read) holds the input
+    # rows and the exits, however the rows travelled
+    _, PsiB_dev = umtlib.get_psi(capi.UMT_FP32)
+    assert np.array_equal(PsiB_dev[kept], PsiB0[kept].astype(np.float32).astype(np.float64))
+    assert np.array_equal(PsiB_dev[~kept], PsiB[~kept])
 
 
 def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):

@@ -72,7 +72,7 @@ static void free_ctx(Ctx &c) {
   dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
-  dfree(c.psibOut);
+  dfree(c.psibOut); dfree(c.phiOut);
   c.stage64N = 0;
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
@@ -379,6 +379,7 @@ static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int fla
     for (int i = 0; i < 2; ++i) { TRY(dalloc(&c.psi32[i], psiN)); UMT_CUDA(cudaMemset(c.psi32[i], 0, psiN * 4)); }
     TRY(dalloc(&c.psiB32, psiBN)); UMT_CUDA(cudaMemset(c.psiB32, 0, psiBN * 4));
     TRY(dalloc(&c.psibOut, 1)); UMT_CUDA(cudaMemset(c.psibOut, 0, sizeof(double *)));
+    TRY(dalloc(&c.phiOut, 1)); UMT_CUDA(cudaMemset(c.phiOut, 0, sizeof(double *)));
   }
   UMT_CUDA(cudaDeviceSynchronize());
   c.ready = true;
@@ -585,15 +586,22 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
   if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
   else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
-  // FP32: only the rows a sweep reads go in and only the rows it writes come
-  // out, so the caller's array keeps its other rows bit for bit.  Page-locked
-  // host memory is read and written by the row kernels directly; pageable
-  // memory goes through the FP64 staging buffer, which keeps the input rows.
-  double *psibHost = nullptr, *psibFP64 = nullptr;
-  if (PsiB_inout) {
-    if (precision == UMT_FP64) {
-      UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
-    } else {
+  // FP32: only the PsiB rows a sweep reads go in and only the rows it writes
+  // come out, so the caller's array keeps its other rows bit for bit.
+  // Page-locked host memory is read and written by the kernels directly;
+  // pageable memory goes through the FP64 staging buffer, which keeps the
+  // input rows.  The incoming rows are converted into the device copy before
+  // the sweep (reading them from host memory inside the stage kernels put
+  // the link's latency on every boundary item's dependency chain and was
+  // slower).  With the zone-program kernel the sweep writes the exiting rows
+  // to the FP64 array as it goes (its host-facing variant), and the tally
+  // writes PhiTotal straight to a page-locked destination.
+  double *psibHost = nullptr, *psibFP64 = nullptr, *phiHost = nullptr;
+  bool psibWT = false, wt = false;
+  if (precision == UMT_FP32 && (PsiB_inout || PhiTotal_out)) {
+    bool prog = false;
+    TRY(fp32_program_path(c, &prog));
+    if (PsiB_inout) {
       TRY(ensure_bface(c));
       psibHost = mapped_host(PsiB_inout);
       psibFP64 = psibHost;
@@ -601,20 +609,33 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
         TRY(staging64(c, psiBN, &psibFP64));
         UMT_CUDA(cudaMemcpyAsync(psibFP64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
       }
-      k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, psibFP64, c.psiB32, nullptr, 0);
-      // the zone-program kernel writes exiting rows straight to the FP64
-      // destination during the sweep (16-byte stores: needs a 16-byte base)
-      c.wantExitsThrough = ((uintptr_t)psibFP64 & 15u) == 0;
-      k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, c.wantExitsThrough ? psibFP64 : nullptr);
-      UMT_CUDA(cudaGetLastError());
+      psibWT = prog && ((uintptr_t)psibFP64 & 15u) == 0;      // the kernel's FP64 accesses are 16-byte
     }
+    if (PhiTotal_out) {
+      phiHost = mapped_host(PhiTotal_out);
+      if ((uintptr_t)phiHost & 15u) phiHost = nullptr;
+    }
+    wt = psibWT || phiHost;
+    if (PsiB_inout)
+      k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, psibFP64, c.psiB32, nullptr, 0);
+    if (wt) {
+      k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, psibWT ? psibFP64 : nullptr);
+      k_set_word<<<1, 1, 0, c.stream>>>(c.phiOut, phiHost);
+    }
+    UMT_CUDA(cudaGetLastError());
+  } else if (PsiB_inout) {
+    UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
   }
+  c.wantExitsThrough = wt;
   const int rcs = sweep_core(savePsi, precision);
-  const bool wrote = c.wantExitsThrough && c.exitsThrough;
+  const bool wrote = psibWT && c.exitsThrough;
   c.wantExitsThrough = false;
-  if (psibFP64) k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, nullptr);   // resident sweeps write nothing
+  if (wt) {                                        // resident sweeps write nothing to the host
+    k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, nullptr);
+    k_set_word<<<1, 1, 0, c.stream>>>(c.phiOut, nullptr);
+  }
   TRY(rcs);
-  if (PhiTotal_out) UMT_CUDA(cudaMemcpyAsync(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (PhiTotal_out && !phiHost) UMT_CUDA(cudaMemcpyAsync(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));
   if (PsiB_inout) {
     if (precision == UMT_FP64) {
       UMT_CUDA(cudaMemcpyAsync(PsiB_inout, c.psiB64, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));

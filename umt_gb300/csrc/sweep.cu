@@ -213,10 +213,15 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float w, float x) 
   s = t;
 }
 
+// WT: PhiTotal also goes to *phiOut (the caller's page-locked array) when set.
+template <bool WT>
 __global__ void __launch_bounds__(256) k_tally32(int A, size_t ncG, const float *__restrict__ w32,
-                                                 const float *__restrict__ psi, double *__restrict__ Phi) {
-  constexpr int U = 16;                       // float4 loads in flight per thread
+                                                 const float *__restrict__ psi, double *__restrict__ Phi,
+                                                 double *const *phiOut) {
+  constexpr int U = 16;                       // float4 loads per thread per step
   const size_t n4 = ncG / 4;
+  double *host = nullptr;
+  if constexpr (WT) host = *phiOut;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n4; q += (size_t)gridDim.x * blockDim.x) {
     float s[4] = {0.f, 0.f, 0.f, 0.f}, c[4] = {0.f, 0.f, 0.f, 0.f};
     const float *p = psi + 4 * q;
@@ -225,7 +230,7 @@ __global__ void __launch_bounds__(256) k_tally32(int A, size_t ncG, const float 
       float4 v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) v[u] = *reinterpret_cast<const float4 *>(p + (size_t)(a + u) * ncG);
-      asm volatile("" ::: "memory");          // issue all U loads before the first sum
+      asm volatile("" ::: "memory");          // compiler barrier between the loads and the sums
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const float w = w32[a + u];
@@ -239,15 +244,24 @@ __global__ void __launch_bounds__(256) k_tally32(int A, size_t ncG, const float 
       kahan_add(s[0], c[0], w, v.x); kahan_add(s[1], c[1], w, v.y);
       kahan_add(s[2], c[2], w, v.z); kahan_add(s[3], c[3], w, v.w);
     }
-    *reinterpret_cast<double2 *>(Phi + 4 * q) =
-        make_double2((double)s[0] - (double)c[0], (double)s[1] - (double)c[1]);
-    *reinterpret_cast<double2 *>(Phi + 4 * q + 2) =
-        make_double2((double)s[2] - (double)c[2], (double)s[3] - (double)c[3]);
+    const double2 lo = make_double2((double)s[0] - (double)c[0], (double)s[1] - (double)c[1]);
+    const double2 hi = make_double2((double)s[2] - (double)c[2], (double)s[3] - (double)c[3]);
+    *reinterpret_cast<double2 *>(Phi + 4 * q) = lo;
+    *reinterpret_cast<double2 *>(Phi + 4 * q + 2) = hi;
+    if constexpr (WT) {
+      if (host) {
+        *reinterpret_cast<double2 *>(host + 4 * q) = lo;
+        *reinterpret_cast<double2 *>(host + 4 * q + 2) = hi;
+      }
+    }
   }
   for (size_t e = 4 * n4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < ncG; e += (size_t)gridDim.x * blockDim.x) {
     double t = 0.0;
     for (int a = 0; a < A; ++a) t += (double)(w32[a] * psi[(size_t)a * ncG + e]);
     Phi[e] = t;
+    if constexpr (WT) {
+      if (host) host[e] = t;
+    }
   }
 }
 
@@ -355,11 +369,26 @@ static int enqueue_sweep(Ctx &c, int cur) {
   TRY_RC(record_mid(c));
   const size_t ncG = (size_t)c.nc * c.G;
   const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
-  if constexpr (sizeof(T) == 4)
-    k_tally32<<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi);
-  else
+  if constexpr (sizeof(T) == 4) {
+    if (c.wantExitsThrough)
+      k_tally32<true><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi, c.phiOut);
+    else
+      k_tally32<false><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi, nullptr);
+  } else {
     k_tally<double><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight, c.psi64[1 - cur], c.Phi);
+  }
   UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static int prepare_precision(Ctx &c, int precision);
+
+// Whether an FP32 sweep of this context runs the zone-program kernel (the
+// kernel with the host-facing variant); prepares the FP32 records first.
+int fp32_program_path(Ctx &c, bool *yes) {
+  TRY_RC(prepare_precision(c, 1));
+  *yes = c.sweepMode == 0 && c.progState == 1 && c.tileGT > 0 && sweep32_supported(c.G, c.tileGT, c.tileGPL) &&
+         sweep32p_supported(c.G, c.tileGT, c.tileGPL);
   return 0;
 }
 
@@ -369,7 +398,7 @@ int launch_tally(Ctx &c, int precision) {
   const size_t ncG = (size_t)c.nc * c.G;
   const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
   if (precision == 1)
-    k_tally32<<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - c.cur32], c.Phi);
+    k_tally32<false><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - c.cur32], c.Phi, nullptr);
   else
     k_tally<double><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight, c.psi64[1 - c.cur64], c.Phi);
   UMT_CUDA(cudaGetLastError());

@@ -107,8 +107,6 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   unsigned char *sB = reinterpret_cast<unsigned char *>(smem4) + (size_t)TEAMS * p.tstride * 4 +
                       (size_t)team * p.bstride;
   const uint4 h = p.hdr[p.stageOffset[stage] + k];
-  double *hb = nullptr;
-  if constexpr (WT) hb = *p.psibOut;               // read with the header: off the exit path's chain
   const bool bad = (h.x >> 31) != 0;
   const uint32_t it = h.x & 0x7fffffffu;
   const int a = (int)(((unsigned long long)it * p.nzMagic) >> p.nzShift);
@@ -289,7 +287,12 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   // exiting boundary fluxes; with WT the same rows also go, in FP64, to the
   // caller's PsiB (page-locked host memory) or its staging copy when one is set
   double *hbA = nullptr;
-  if constexpr (WT) hbA = hb ? hb + (size_t)a * p.nb * G + g0 : nullptr;
+  if constexpr (WT) {
+    if (nX) {
+      double *const hb = *p.psibOut;             // read here: nothing stays live across the solve
+      hbA = hb ? hb + (size_t)a * p.nb * G + g0 : nullptr;
+    }
+  }
   for (int x = 0; x < nX; ++x) {
     const uint32_t e = ex[x];
     float2 v[NP];

@@ -98,11 +98,12 @@ struct Ctx {
   double *scratch = nullptr;                    // reductions
   size_t scratchBytes = 0;
   int *bFace = nullptr;                         // [nb] corner face c*3 + f of each boundary element (-1: none)
-  double **psibOut = nullptr;                   // device word read by the zone-program kernel: FP64
-                                                // destination of the exiting PsiB rows, or null
+  double **psibOut = nullptr;                   // device word read by the zone-program kernel's host-facing
+                                                // variant: FP64 destination of the exiting PsiB rows, or null
+  double **phiOut = nullptr;                    // device word: FP64 PhiTotal destination of the tally, or null
   bool exitsThrough = false;                    // the FP32 sweep as enqueued runs the zone-program kernel
-  bool wantExitsThrough = false;                // enqueue its variant that writes *psibOut
-  cudaGraphExec_t graphsWT[2] = {nullptr, nullptr};   // FP32 sweeps of that variant, [cur]
+  bool wantExitsThrough = false;                // enqueue the host-facing variants (zone program, tally)
+  cudaGraphExec_t graphsWT[2] = {nullptr, nullptr};   // FP32 sweeps of those variants, [cur]
   double *stage64 = nullptr;                    // FP64 staging of PsiB for FP32 sweeps (kept)
   size_t stage64N = 0;
   // captured sweep graphs per precision
@@ -166,6 +167,8 @@ void default_tile(int G, int *GT, int *GPL);
 void free_rz(Ctx &c);
 // persistent FP64 staging buffer of at least n elements (capi.cu)
 int staging_buffer64(Ctx &c, size_t n, double **out);
+// whether an FP32 sweep runs the zone-program kernel (sweep.cu)
+int fp32_program_path(Ctx &c, bool *yes);
 // zone-program FP32 kernel (sweep32p.cu)
 int prepare_prog32(Ctx &c);
 bool sweep32p_supported(int G, int GT, int GPL);
