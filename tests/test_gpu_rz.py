@@ -81,7 +81,8 @@ def test_rz_repeated_sweeps_and_source_iteration(umtlib):
 FP32_PHI_TOL, FP32_PSI_TOL = 2e-5, 1e-4
 
 
-@pytest.mark.parametrize("nr,nzr,P,Az,G,index_base", [(6, 5, 4, 3, 8, 0), (7, 6, 2, 4, 16, 1), (3, 4, 1, 2, 3, 0)])
+@pytest.mark.parametrize("nr,nzr,P,Az,G,index_base", [(6, 5, 4, 3, 8, 0), (7, 6, 2, 4, 16, 1), (3, 4, 1, 2, 3, 0),
+                                                    (3, 3, 1, 2, 40, 0)])
 def test_rz_fp32_sweep_matches_oracle(umtlib, nr, nzr, P, Az, G, index_base):
     m, q, sigt, STotal, psi0, PsiB = _problem(nr, nzr, P, Az, G, seed=nr * 7 + G)
     tau = 0.7

@@ -158,15 +158,19 @@ def test_batch_of_contexts_matches_single_runs(umtlib):
         umtlib.context_destroy(cid)
 
 
-@pytest.mark.parametrize("pinned", [False, True])
-def test_fp32_sweep_writes_only_exiting_psib_rows(umtlib, pinned):
+@pytest.mark.parametrize("memory", ["pageable", "pinned", "pinned_unaligned"])
+@pytest.mark.parametrize("G", [8, 3])
+def test_fp32_sweep_writes_only_exiting_psib_rows(umtlib, memory, G):
     """An FP32 sweep writes the caller's PsiB only on exiting rows, as the
     reference writes PsiB only on the exit list: every row the oracle leaves
     unchanged keeps its FP64 input bit for bit, exiting rows agree with the
-    oracle to the FP32 tolerance, and umt103_psib_rows counts them."""
-    prob = synthetic_problem((3, 2, 2), 2, 2, 8, seed=4, time_dependent=True)
+    oracle to the FP32 tolerance, and umt103_psib_rows counts them.  G = 3 runs
+    the generic FP32 kernel (no zone programs), and a page-locked array that
+    is not 16-byte aligned takes the row-kernel path instead of the stage
+    kernels' FP64 stores."""
+    prob = synthetic_problem((3, 2, 2), 2, 2, G, seed=4, time_dependent=True)
     m = prob.mesh
-    A, G = len(prob.weight), prob.ngr
+    A = len(prob.weight)
     rng = np.random.default_rng(5)
     PsiB0 = rng.uniform(0.0, 0.1, size=(A, m.nbelem, G))
     STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
@@ -174,11 +178,14 @@ def test_fp32_sweep_writes_only_exiting_psib_rows(umtlib, pinned):
     umtlib.init(m, prob.omega, prob.weight, G)
     umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
     umtlib.set_psi(prob.psi0, None)
-    if pinned:
-        torch = pytest.importorskip("torch")
-        PsiB = torch.empty((A, m.nbelem, G), dtype=torch.float64, pin_memory=True).numpy()
-    else:
+    if memory == "pageable":
         PsiB = np.empty((A, m.nbelem, G))
+    else:
+        torch = pytest.importorskip("torch")
+        n = A * m.nbelem * G
+        buf = torch.empty(n + 1, dtype=torch.float64, pin_memory=True).numpy()
+        PsiB = (buf[1:] if memory == "pinned_unaligned" else buf[:n]).reshape(A, m.nbelem, G)
+        assert (PsiB.ctypes.data % 16 != 0) == (memory == "pinned_unaligned")
     PsiB[...] = PsiB0
     Phi = umtlib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=capi.UMT_FP32)
     kept = np.all(ref["PsiB"] == PsiB0, axis=2)                  # rows the oracle did not write
