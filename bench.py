@@ -10,7 +10,12 @@ ratio uniform on [0, 0.5], isotropic source 1.0, vacuum boundaries, seeded
 stand in for the reference's problem; there is no dataset.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--tiles T] [--precision fp32|fp64]
+                    [--tiles T] [--precision fp32|fp64] [--config 2|3] [--rz]
+
+--config 3 is the larger scattering problem: 30^3 tiles, four materials by
+tile (seed 3), total opacity log-uniform on [1e-3, 1e3], scattering ratio up
+to 0.9.  --rz times the 2-D RZ sweep instead (200 x 200 quadrilaterals, 144
+directions, 16 groups).
 
 Multi-GPU: the sweep of one problem does not shard here, so N GPUs run N
 independent replicas (one process per GPU, launched by torchrun); value is
@@ -121,8 +126,18 @@ def dist_setup():
     return world, rank, local
 
 
-def make_problem(tiles):
+MATERIALS = {2: "sigma_t log-uniform on [1e-2, 1e2] per zone and group (seed 2), c ~ U[0, 0.5]",
+             3: "4 materials by tile (seed 3), sigma_t log-uniform on [1e-3, 1e3], c ~ U[0, 0.9]"}
+
+
+def make_problem(tiles, config=2):
+    """The scattering workloads: 128 directions (P = Az = 4), 16 groups, q = 1,
+    tau = 1/(c dt) with dt = 1e-3; config 2 draws opacities per zone, config 3
+    per material with a per-tile material index."""
     from umt_gb300.problems import synthetic_problem
+    if config == 3:
+        return synthetic_problem((tiles,) * 3, 4, 4, 16, seed=3, sigt_range=(1e-3, 1e3), c_range=(0.0, 0.9),
+                                 q=1.0, n_materials=4, time_dependent=True)
     return synthetic_problem((tiles,) * 3, 4, 4, 16, seed=2, sigt_range=(1e-2, 1e2), c_range=(0.0, 0.5),
                              q=1.0, time_dependent=True)
 
@@ -139,7 +154,7 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     from oracle import pyoracle as po
-    prob = make_problem(args.tiles)
+    prob = make_problem(args.tiles, args.config)
     m = prob.mesh
     A, G = len(prob.weight), prob.ngr
     nth = os.cpu_count() or 1
@@ -166,7 +181,7 @@ def run_reference(args, world, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"multigroup scattering, {args.tiles}^3 tiles, 128 directions, 16 groups",
-                       "tiles": args.tiles, "directions": A, "groups": G, "zones": m.nzones,
+                       "materials": MATERIALS[args.config], "tiles": args.tiles, "directions": A, "groups": G, "zones": m.nzones,
                        "corners": m.ncornr, "sample_directions": int(sample_angles)},
             "cpu_baseline": {"value": v, "unit": "ns", "cores": nth, "kind": "port",
                              "sample": f"{sample_angles} of {A} directions on the full mesh, all groups"},
@@ -307,15 +322,19 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--tiles", type=int, default=20)
+    ap.add_argument("--tiles", type=int, default=None, help="tiles per axis (default 20, or 30 for --config 3)")
+    ap.add_argument("--config", type=int, default=2, choices=(2, 3),
+                    help="2: opacities per zone (default); 3: four materials by tile, c up to 0.9")
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
-    ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (FP64)")
+    ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (precision as --precision)")
     ap.add_argument("--rz-cells", type=int, default=200, help="RZ mesh: cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.tiles is None:
+        args.tiles = 30 if args.config == 3 else 20
     world, rank, local = dist_setup()
     if args.rz:
         if rank == 0:
@@ -337,7 +356,7 @@ def main():
     lib = capi.Library()
     lib.select_device(local)
     prec = capi.UMT_FP32 if args.precision == "fp32" else capi.UMT_FP64
-    prob = make_problem(args.tiles)
+    prob = make_problem(args.tiles, args.config)
     m = prob.mesh
     A, G = len(prob.weight), prob.ngr
     lib.init(m, prob.omega, prob.weight, G, flags=3 if world == 1 and not args.no_ttc else
@@ -421,6 +440,7 @@ def main():
         "vs_baseline": None, "dtype": "f32" if prec == capi.UMT_FP32 else "f64", "data": "synthetic",
         "config": {"workload": f"multigroup scattering sweep, {args.tiles}^3 tiles (24-zone tile), "
                                f"128 directions, 16 groups",
+                   "materials": MATERIALS[args.config],
                    "tiles": args.tiles, "zones": m.nzones, "corners": m.ncornr, "directions": A,
                    "groups": G, "units_per_step": units, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2 (angular flux %.1f GB)" % (A * m.ncornr * G * s / 1e9),
