@@ -27,6 +27,21 @@ def test_uniform_problem_cycles_fp64(umtlib):
         assert abs(e["EnergyCheckClosed"]) < 1e-11 * e["EnergyRadiation"]
 
 
+def test_config1_ten_cycles_fp64(umtlib):
+    """The reference driver's uniform problem at its full size (10^3 tiles,
+    24,000 zones, 32 directions, 2 groups) for 10 cycles, every cycle against
+    the oracle: PhiTotal, radiation energy, escape and the energy check."""
+    prob = uniform_problem((10, 10, 10), 2, 2, 2)
+    ref = oracle_cycles(prob, 10)
+    t = Teton(prob, capi.UMT_FP64, umtlib)
+    for k in range(10):
+        e = t.radtr()
+        assert rel_err(t.PhiTotal, ref[k]["PhiTotal"]) < 1e-12, k
+        assert abs(e["EnergyRadiation"] / ref[k]["EnergyRadiation"] - 1) < 1e-12, k
+        assert abs(e["PowerEscape"] / ref[k]["PowerEscape"] - 1) < 1e-12, k
+        assert abs(e["EnergyCheck"] - ref[k]["EnergyCheck"]) < 1e-12 * e["EnergyRadiation"], k
+
+
 def test_uniform_problem_cycles_fp32(umtlib):
     prob = uniform_problem((2, 2, 2), 2, 2, 2)
     ref = oracle_cycles(prob, 2)

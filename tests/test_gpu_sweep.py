@@ -123,12 +123,25 @@ def test_fp32_sweep_modes(umtlib, mode):
         assert rel_err(PsiB, ref["PsiB"]) < 1e-4
 
 
-def test_batch_of_contexts_matches_single_runs(umtlib):
+def _config4_draws(n=12, seed=4):
+    """The batched workload's problem mix: G in {4, 8, 16, 32, 64}, A in
+    {32, 128} (P = Az in {2, 4}); tiles per axis from U{2..4} instead of
+    U{4..16} so that the single-context runs stay short."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        t = int(rng.integers(2, 5))
+        out.append(((t, t, t), int(rng.choice([2, 4])), int(rng.choice([4, 8, 16, 32, 64])), 400 + k))
+    return out
+
+
+@pytest.mark.parametrize("specs", [[((2, 2, 1), 2, 4, 31), ((3, 2, 1), 4, 8, 32), ((2, 3, 2), 2, 16, 33)],
+                                   _config4_draws()], ids=["three", "config4_draws"])
+def test_batch_of_contexts_matches_single_runs(umtlib, specs):
     """Several problems of different size, group and direction counts resident
     in separate contexts, swept from one graph launch, give each problem's
     single-context result."""
     from umt_gb300.problems import synthetic_problem as sp
-    specs = [((2, 2, 1), 2, 4, 31), ((3, 2, 1), 4, 8, 32), ((2, 3, 2), 2, 16, 33)]
     probs = [sp(t, P, P, G, seed=s, time_dependent=True) for (t, P, G, s) in specs]
     single = []
     for pr in probs:
