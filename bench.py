@@ -405,9 +405,12 @@ def main():
         lib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=prec, Phi=Phi)
     barrier()
     e2e_steps = max(3, min(args.steps, 10))
+    call_ms = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        tc = time.perf_counter()
         lib.sweep(STotal, savePsi=False, PsiB=PsiB, precision=prec, Phi=Phi)
+        call_ms.append((time.perf_counter() - tc) * 1e3)
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     barrier()
     if dist:
@@ -456,7 +459,9 @@ def main():
                 "call": "umt103_sweep(STotal, savePsi=0, PhiTotal, PsiB inout, %s)" %
                         ("FP32" if prec == capi.UMT_FP32 else "FP64"),
                 "psib": ("rows the sweep reads in, rows it writes out (FP64 host array)"
-                         if prec == capi.UMT_FP32 else "whole array both ways")},
+                         if prec == capi.UMT_FP32 else "whole array both ways"),
+                "call_ms": {"min": min(call_ms), "median": statistics.median(call_ms), "max": max(call_ms),
+                            "calls": len(call_ms)}},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
     }

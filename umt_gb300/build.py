@@ -28,6 +28,7 @@ UNITS = {
     "si.cu": [],
     "rz.cu": ["-Xcompiler", "-ffp-contract=off"],   # host-side RZ geometry, same rounding as the Fortran
     "noalloc.cu": [],
+    "psib.cu": [],
 }
 
 

@@ -73,6 +73,7 @@ static void free_ctx(Ctx &c) {
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
   dfree(c.psibOut); dfree(c.phiOut);
+  free_psib(c);
   c.stage64N = 0;
   if (c.ev0) cudaEventDestroy(c.ev0);
   if (c.ev1) cudaEventDestroy(c.ev1);
@@ -410,16 +411,6 @@ __global__ void k_f2d(size_t n, const float *x, double *y) {
     y[i] = (double)x[i];
 }
 
-// Boundary element b's corner face c*3 + f (cFP holds nc + b on boundary faces).
-__global__ void k_bface(int nc, int nb, const int *nCFaces, const int *cFP, int *bFace) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nc) return;
-  for (int f = 0; f < nCFaces[c]; ++f) {
-    const int v = cFP[c * UMT_MAXCF + f];
-    if (v >= nc && v - nc < nb) bFace[v - nc] = c * UMT_MAXCF + f;
-  }
-}
-
 // PsiB rows (direction a, boundary element b; G values each) as the FP32
 // sweep kernels classify them: a row is exiting when the FP32 projection
 // Omega_a.A_fp of b's corner face is > 0 (the sweep writes it), every other
@@ -449,16 +440,6 @@ __global__ void k_count_exit_rows(int A, int nb, int nc, const int *bFace, const
     k += (bf >= 0 && afp32[(size_t)a * nc * UMT_MAXCF + bf] > 0.f) ? 1 : 0;
   }
   if (k) atomicAdd(count, k);
-}
-
-static int ensure_bface(Ctx &c) {
-  if (c.bFace) return 0;
-  TRY(dalloc(&c.bFace, std::max(c.nb, 1)));
-  UMT_CUDA(cudaMemset(c.bFace, 0xff, (size_t)std::max(c.nb, 1) * sizeof(int)));
-  k_bface<<<(c.nc + 255) / 256, 256>>>(c.nc, c.nb, c.nCFaces, c.cFP, c.bFace);
-  UMT_CUDA(cudaGetLastError());
-  UMT_CUDA(cudaDeviceSynchronize());
-  return 0;
 }
 
 __global__ void k_set_word(double **word, double *value) { *word = value; }
@@ -590,12 +571,13 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   // come out, so the caller's array keeps its other rows bit for bit.
   // Page-locked host memory is read and written by the kernels directly;
   // pageable memory goes through the FP64 staging buffer, which keeps the
-  // input rows.  The incoming rows are converted into the device copy before
-  // the sweep (reading them from host memory inside the stage kernels put
-  // the link's latency on every boundary item's dependency chain and was
-  // slower).  With the zone-program kernel the sweep writes the exiting rows
-  // to the FP64 array as it goes (its host-facing variant), and the tally
-  // writes PhiTotal straight to a page-locked destination.
+  // input rows.  The incoming rows are converted into the device copy, not
+  // read from host memory by the stage kernels (that put the link's latency
+  // on every boundary item's dependency chain and was slower).  With the
+  // zone-program kernel that copy runs in stage-ordered chunks beside the
+  // stages, the sweep writes the exiting rows to the FP64 array as it goes
+  // (its host-facing variant), and the tally writes PhiTotal straight to a
+  // page-locked destination.
   double *psibHost = nullptr, *psibFP64 = nullptr, *phiHost = nullptr;
   bool psibWT = false, wt = false;
   if (precision == UMT_FP32 && (PsiB_inout || PhiTotal_out)) {
@@ -616,9 +598,13 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
       if ((uintptr_t)phiHost & 15u) phiHost = nullptr;
     }
     wt = psibWT || phiHost;
-    if (PsiB_inout)
+    // the host-facing graph copies the rows the sweep reads in stage-ordered
+    // chunks beside the stages (psib.cu); otherwise they go in first
+    if (wt) TRY(ensure_psib_order(c));
+    if (PsiB_inout && !psibWT)
       k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, psibFP64, c.psiB32, nullptr, 0);
     if (wt) {
+      k_set_word<<<1, 1, 0, c.stream>>>(c.psibIn, psibWT ? psibFP64 : nullptr);
       k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, psibWT ? psibFP64 : nullptr);
       k_set_word<<<1, 1, 0, c.stream>>>(c.phiOut, phiHost);
     }
@@ -630,7 +616,8 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   const int rcs = sweep_core(savePsi, precision);
   const bool wrote = psibWT && c.exitsThrough;
   c.wantExitsThrough = false;
-  if (wt) {                                        // resident sweeps write nothing to the host
+  if (wt) {                                        // resident sweeps touch no host memory
+    k_set_word<<<1, 1, 0, c.stream>>>(c.psibIn, nullptr);
     k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, nullptr);
     k_set_word<<<1, 1, 0, c.stream>>>(c.phiOut, nullptr);
   }

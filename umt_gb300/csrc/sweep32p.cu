@@ -721,11 +721,23 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   if (GT == gt && GPL == gpl) {                                                                \
     void (*kern)(ProgP, int) = c.wantExitsThrough ? k_sweep32p<gt, gpl, true>                  \
                                                   : k_sweep32p<gt, gpl, false>;                \
+    if (c.wantExitsThrough) {                                                                  \
+      const int rq = enqueue_psib_chunks(c);                                                   \
+      if (rq) return rq;                                                                       \
+    }                                                                                          \
     for (int s = 0; s < c.sch.nStages; ++s) {                                                  \
+      if (c.wantExitsThrough) {                                                                \
+        const int rq = wait_psib_chunks(c, s);                                                 \
+        if (rq) return rq;                                                                     \
+      }                                                                                        \
       cfg.gridDim = dim3((c.sch.hCount[s] + TEAMS - 1) / TEAMS);                               \
       cfg.attrs = s > 0 && c.usePDL ? pdl : nullptr;                                           \
       cfg.numAttrs = s > 0 && c.usePDL ? 1 : 0;                                                \
       UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p, s));                                          \
+    }                                                                                          \
+    if (c.wantExitsThrough) {                                                                  \
+      const int rq = wait_psib_chunks(c, c.sch.nStages);                                       \
+      if (rq) return rq;                                                                       \
     }                                                                                          \
     return 0;                                                                                  \
   }

@@ -104,6 +104,14 @@ struct Ctx {
   bool exitsThrough = false;                    // the FP32 sweep as enqueued runs the zone-program kernel
   bool wantExitsThrough = false;                // enqueue the host-facing variants (zone program, tally)
   cudaGraphExec_t graphsWT[2] = {nullptr, nullptr};   // FP32 sweeps of those variants, [cur]
+  // PsiB rows the sweep does not write, ordered by the stage that reads them
+  // (psib.cu), copied in chunks on a side stream inside the host-facing graph
+  int *rowOrder = nullptr;                      // row indices a*nb + b
+  std::vector<int> chunkOff, chunkStage;        // chunk k: rowOrder[chunkOff[k], chunkOff[k+1]), read from stage chunkStage[k]
+  double **psibIn = nullptr;                    // device word: the FP64 rows to copy (host or staging), or null
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t evFork = nullptr;
+  std::vector<cudaEvent_t> evChunk;
   double *stage64 = nullptr;                    // FP64 staging of PsiB for FP32 sweeps (kept)
   size_t stage64N = 0;
   // captured sweep graphs per precision
@@ -169,6 +177,12 @@ void free_rz(Ctx &c);
 int staging_buffer64(Ctx &c, size_t n, double **out);
 // whether an FP32 sweep runs the zone-program kernel (sweep.cu)
 int fp32_program_path(Ctx &c, bool *yes);
+// PsiB rows between host arrays and the device copy (psib.cu)
+int ensure_bface(Ctx &c);
+int ensure_psib_order(Ctx &c);
+int enqueue_psib_chunks(Ctx &c);
+int wait_psib_chunks(Ctx &c, int stage);
+void free_psib(Ctx &c);
 // zone-program FP32 kernel (sweep32p.cu)
 int prepare_prog32(Ctx &c);
 bool sweep32p_supported(int G, int GT, int GPL);
