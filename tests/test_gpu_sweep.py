@@ -219,14 +219,16 @@ def test_fp32_sweep_writes_only_exiting_psib_rows(umtlib, memory, G):
 def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):
     """Page-locked and pageable host arrays give bit-identical sweeps, with
     incoming boundary fluxes set and exits returned (the bench passes
-    page-locked buffers)."""
+    page-locked buffers, whose STotal and PsiB rows arrive in stage-ordered
+    chunks beside the stages); the source the call leaves on the device
+    drives the next resident sweep identically."""
     torch = pytest.importorskip("torch")
     prob = synthetic_problem((3, 2, 2), 2, 2, 8, seed=9, time_dependent=True)
     m = prob.mesh
     A, G = len(prob.weight), prob.ngr
     rng = np.random.default_rng(3)
     PsiB0 = rng.uniform(0.0, 0.1, size=(A, m.nbelem, G))
-    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    STotal0 = rng.uniform(0.05, 1.0, size=(m.ncornr, G))
     out = []
     for pinned in (False, True):
         umtlib.init(m, prob.omega, prob.weight, G, flags=2 | 8)
@@ -235,12 +237,17 @@ def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):
         if pinned:
             PsiB = torch.empty((A, m.nbelem, G), dtype=torch.float64, pin_memory=True).numpy()
             Phi = torch.empty((m.ncornr, G), dtype=torch.float64, pin_memory=True).numpy()
+            STotal = torch.empty((m.ncornr, G), dtype=torch.float64, pin_memory=True).numpy()
         else:
             PsiB = np.empty((A, m.nbelem, G))
             Phi = np.empty((m.ncornr, G))
+            STotal = np.empty((m.ncornr, G))
         PsiB[...] = PsiB0
+        STotal[...] = STotal0
         umtlib.sweep(STotal, savePsi=True, PsiB=PsiB, precision=capi.UMT_FP32, Phi=Phi)
-        out.append((Phi.copy(), PsiB.copy()))
+        umtlib.sweep_resident(False, capi.UMT_FP32)
+        out.append((Phi.copy(), PsiB.copy(), umtlib.get_phi(m.ncornr, G)))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2])
     assert not np.array_equal(out[1][1], PsiB0)                   # exits were written back
