@@ -151,6 +151,26 @@ def test_rz_fp32_repeated_sweeps_and_tau_change(umtlib):
     assert rel_err(Psi_d, Psi_o) < FP32_PSI_TOL
 
 
+@pytest.mark.parametrize("precision", [capi.UMT_FP64, capi.UMT_FP32])
+def test_rz_sweep_writes_only_exiting_psib_rows(umtlib, precision):
+    """The caller's PsiB changes only on the rows the sweep writes (exits,
+    and a finishing direction's rows on its predecessor's exits): every row
+    the oracle leaves unchanged keeps its FP64 input bit for bit."""
+    m, q, sigt, STotal, psi0, PsiB = _problem(5, 4, 2, 3, 8, seed=21)
+    tau = 0.6
+    geo, Phi_ref, Psi_ref, PsiB_ref = _oracle(m, q, sigt, STotal, psi0, PsiB, tau)
+    umtlib.init_rz(m, q, 8)
+    umtlib.set_materials(sigt, np.zeros_like(sigt), tau)
+    umtlib.set_psi(psi0, None)
+    PB = PsiB.copy()
+    umtlib.sweep_rz(STotal, savePsi=True, PsiB=PB, precision=precision)
+    kept = np.all(PsiB_ref == PsiB, axis=2)
+    assert kept.any() and (~kept).any()
+    assert np.array_equal(PB[kept], PsiB[kept])
+    tol = 1e-12 if precision == capi.UMT_FP64 else FP32_PSI_TOL
+    assert rel_err(PB[~kept], PsiB_ref[~kept]) < tol
+
+
 def test_rz_precision_refusals(umtlib):
     m, q, sigt, STotal, psi0, PsiB = _problem(2, 3, 1, 1, 2, seed=4)
     umtlib.init_rz(m, q, 2, flags=1)                     # FP64 flux only

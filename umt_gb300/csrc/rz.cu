@@ -45,6 +45,7 @@ struct RZData {
   int2 *link32 = nullptr;                    // [nc] {cFP0 << 3 | cEZ0, cFP1 << 3 | cEZ1}
   float *fac32 = nullptr, *W1_32 = nullptr, *W2_32 = nullptr;   // [A]
   float *PsiM32 = nullptr;                   // [nLevels][nc][G]
+  int *bFace2 = nullptr;                     // [nb] corner face 2*c + f of each boundary element (-1: none)
   cudaGraphExec_t graph32[2] = {nullptr, nullptr};   // one FP32 sweep per buffer parity
   double graphTau = 0.0;
 };
@@ -62,7 +63,7 @@ void free_rz(Ctx &c) {
                   (void *)r->W2, (void *)r->starting, (void *)r->nextFinishing, (void *)r->level, (void *)r->cFP2,
                   (void *)r->cEZ2, (void *)r->PsiM, (void *)r->items, (void *)r->recA, (void *)r->recB,
                   (void *)r->corner32, (void *)r->link32, (void *)r->fac32, (void *)r->W1_32, (void *)r->W2_32,
-                  (void *)r->PsiM32})
+                  (void *)r->PsiM32, (void *)r->bFace2})
     if (p) cudaFree(p);
   delete r;
   c.rz = nullptr;
@@ -318,9 +319,31 @@ __global__ void k_rz_to_float(size_t n, const double *x, float *y) {
     y[i] = (float)x[i];
 }
 
-__global__ void k_rz_to_double(size_t n, const float *x, double *y) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    y[i] = (double)x[i];
+// Boundary element b's corner face 2*c + f (cFP2 holds nc + b on boundary faces).
+__global__ void k_rz_bface(int nc, int nb, const int *cFP2, int *bFace2) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int f = 0; f < 2; ++f) {
+    const int v = cFP2[2 * c + f];
+    if (v >= nc && v - nc < nb) bFace2[v - nc] = 2 * c + f;
+  }
+}
+
+// The PsiB rows an RZ sweep writes, FP32 copy -> FP64 array: row (a, b) when
+// b's corner face exits in direction a, or, for a finishing direction a (not
+// swept), in direction a - 1, whose exits also hand it their PsiM.  Every
+// other row of the FP64 array keeps the caller's value.
+__global__ void k_rz_psib_out(int A, int nb, int nc, int G, const int *bFace2, const double *afp,
+                              const int *nextFinishing, const float *psiB32, double *dst) {
+  const size_t n = (size_t)A * nb * G;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = i / (size_t)G;
+    const int a = (int)(row / (size_t)nb), b = (int)(row - (size_t)a * nb);
+    const int bf = bFace2[b];
+    if (bf < 0) continue;
+    const int as = (a > 0 && nextFinishing[a - 1]) ? a - 1 : a;
+    if (afp[((size_t)as * nc + (bf >> 1)) * UMT_MAXCF + (bf & 1)] > 0.0) dst[i] = (double)psiB32[i];
+  }
 }
 
 struct RZP32 {
@@ -760,9 +783,20 @@ static int sweep_rz32(Ctx &c, RZData &r, int savePsi, double *PhiTotal, double *
   UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
   if (PhiTotal) UMT_CUDA(cudaMemcpyAsync(PhiTotal, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));
   if (PsiB_inout) {
+    // the staging copy still holds the caller's rows: only the written ones change
     double *tmp = nullptr;
     TRY_RC(staging_buffer64(c, psiBN, &tmp));
-    k_rz_to_double<<<4096, 256, 0, c.stream>>>(psiBN, c.psiB32, tmp);
+    if (!r.bFace2) {
+      if (cudaMalloc((void **)&r.bFace2, (size_t)std::max(c.nb, 1) * sizeof(int)) != cudaSuccess) {
+        r.bFace2 = nullptr;
+        return set_error(UMT_ERR_NOMEM, "RZ boundary face map: allocation failed");
+      }
+      UMT_CUDA(cudaMemsetAsync(r.bFace2, 0xff, (size_t)std::max(c.nb, 1) * sizeof(int), c.stream));
+      k_rz_bface<<<(c.nc + 255) / 256, 256, 0, c.stream>>>(c.nc, c.nb, r.cFP2, r.bFace2);
+    }
+    k_rz_psib_out<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, r.bFace2, c.afp64, r.nextFinishing, c.psiB32,
+                                              tmp);
+    UMT_CUDA(cudaGetLastError());
     UMT_CUDA(cudaMemcpyAsync(PsiB_inout, tmp, psiBN * 8, cudaMemcpyDeviceToHost, c.stream));
   }
   UMT_CUDA(cudaStreamSynchronize(c.stream));
