@@ -310,6 +310,15 @@ int umt103_set_sweep_mode(int mode);
 /* Number of kernels one sweep of the given precision launches (>= 0). */
 int umt103_launches_per_sweep(int precision);
 
+/* Failure-path test hook: the next sweep of the current context gives work
+ * item `item` (direction * nzones + zone) one upwind dependency that nothing
+ * satisfies (-1 clears).  In the persistent sweep mode (umt103_set_sweep_mode
+ * 1) that item's bounded wait gives up, every waiting team drains, and the
+ * call returns UMT_ERR_TIMEOUT; the device status is cleared once reported,
+ * so the context stays usable.  Stage-launched modes ignore the hold.  No
+ * counterpart in the reference. */
+int umt103_hold_item(int item);
+
 /* PsiB rows (direction, boundary element) of the current 3-D context: how
  * many the FP32 sweep writes (exiting faces) of the A*nbelem in all.  An FP32
  * umt103_sweep moves only the other rows host -> device and only the

@@ -112,3 +112,34 @@ def test_argument_and_call_order_errors(umtlib):
     # the library stays usable after every refused call
     Phi, _ = _sweep(umtlib, prob, capi.UMT_FP64)
     assert np.isfinite(Phi).all()
+
+
+@pytest.mark.parametrize("item", ["first", "last"])
+def test_persistent_wait_times_out_and_context_recovers(umtlib, item):
+    """Failure detection without a GPU fault: one work item is given an
+    upwind dependency nothing satisfies (a host-side injection).  The
+    persistent sweep's bounded wait gives up, the call returns
+    UMT_ERR_TIMEOUT within about a second, and the next sweep of the same
+    context gives the undisturbed result again."""
+    import time
+    prob = synthetic_problem((2, 2, 1), 2, 2, 8, seed=6, time_dependent=True)
+    m = prob.mesh
+    A = len(prob.weight)
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    umtlib.init(m, prob.omega, prob.weight, prob.ngr, flags=2 | 8)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_sweep_mode(1)
+    umtlib.set_psi(prob.psi0, None)
+    ref = umtlib.sweep(STotal, savePsi=False, precision=capi.UMT_FP32)
+    umtlib.hold_item(0 if item == "first" else A * m.nzones - 1)
+    t0 = time.perf_counter()
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.sweep(STotal, savePsi=False, precision=capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_TIMEOUT
+    assert time.perf_counter() - t0 < 30
+    again = umtlib.sweep(STotal, savePsi=False, precision=capi.UMT_FP32)
+    assert np.array_equal(again, ref)
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.hold_item(A * m.nzones)
+    assert e.value.code == capi.UMT_ERR_ARG
+    umtlib.set_sweep_mode(0)

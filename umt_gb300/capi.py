@@ -95,7 +95,7 @@ def load():
                   "umt103_set_gta", "umt103_tally_noalloc", "umt103_context_create",
                   "umt103_init_rz", "umt103_sweep_rz", "umt103_get_geometry_rz",
                   "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
-                  "umt103_batch_sweep", "umt103_psib_rows"):
+                  "umt103_batch_sweep", "umt103_psib_rows", "umt103_hold_item"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
@@ -113,7 +113,7 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_set_sweep_mode", "umt103_set_gta", "umt103_tally_noalloc",
             "umt103_context_create", "umt103_context_select", "umt103_context_current",
             "umt103_context_destroy", "umt103_batch_sweep", "umt103_init_rz", "umt103_sweep_rz",
-            "umt103_get_geometry_rz", "umt103_psib_rows"]
+            "umt103_get_geometry_rz", "umt103_psib_rows", "umt103_hold_item"]
 
 
 def check(rc):
@@ -289,6 +289,10 @@ class Library:
 
     def set_sweep_mode(self, mode):
         check(self.lib.umt103_set_sweep_mode(int(mode)))
+
+    def hold_item(self, item):
+        """umt103_hold_item: failure-path test hook (see the header)."""
+        check(self.lib.umt103_hold_item(int(item)))
 
     def select_device(self, device):
         check(self.lib.umt103_select_device(int(device)))

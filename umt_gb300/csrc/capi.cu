@@ -510,7 +510,15 @@ static int sweep_core(int savePsi, int precision) {
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
-  TRY(launch_sweep_once(c, precision, true));
+  {
+    // a held item (umt103_hold_item) is enqueued for this sweep only, outside the graphs
+    const bool graphs = c.useGraphs;
+    if (c.holdItem >= 0) c.useGraphs = false;
+    const int rc = launch_sweep_once(c, precision, true);
+    c.useGraphs = graphs;
+    c.holdItem = -1;
+    TRY(rc);
+  }
   UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
   UMT_CUDA(cudaStreamSynchronize(c.stream));
   cudaEventElapsedTime(&c.lastMs, c.ev0, c.ev1);
@@ -525,6 +533,7 @@ static int sweep_core(int savePsi, int precision) {
   }
   unsigned st = 0;
   UMT_CUDA(cudaMemcpy(&st, c.status, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st) UMT_CUDA(cudaMemset(c.status, 0, sizeof(unsigned)));   // reported once; the context stays usable
   if (st & UMT_DEV_BOUNDS) return set_error(UMT_ERR_BOUNDS, "device bounds check");
   if (st & UMT_DEV_TIMEOUT) return set_error(UMT_ERR_TIMEOUT, "device wait timed out");
   return 0;
@@ -648,6 +657,14 @@ int umt103_last_timing(double *out3) {
 int umt103_launches_per_sweep(int precision) {
   if (precision != 0 && precision != 1) return set_error(UMT_ERR_ARG, "precision");
   return cur().launchesPerSweep[precision];
+}
+
+int umt103_hold_item(int item) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (item < -1 || item >= c.A * c.nz) return set_error(UMT_ERR_ARG, "item out of range");
+  c.holdItem = item;
+  return 0;
 }
 
 int umt103_psib_rows(long long *exiting, long long *total) {

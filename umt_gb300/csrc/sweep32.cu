@@ -519,6 +519,10 @@ __global__ void __launch_bounds__(SW32_NT) k_sweep32(Sweep32P p, int stage) {
 // launch always ends and the host reports the error.
 constexpr long long kWaitLimit = 1ll << 22;   // ~0.5 s of polling
 
+// umt103_hold_item: one more upwind zone than the item has, so its wait can
+// only end by the bounded-wait rule (a host-side injection; nothing faults).
+__global__ void k_hold_item(int *dep) { *dep += 1; }
+
 struct PersistP {
   int total;                      // A * nz items
   int *ticket;                    // reset to 0 before the launch
@@ -689,6 +693,7 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   if (c.sweepMode == 1) {
     UMT_CUDA(cudaMemcpyAsync(c.dep, c.sch.needInit, (size_t)q.total * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
     UMT_CUDA(cudaMemsetAsync(c.ticket, 0, sizeof(int), c.stream));
+    if (c.holdItem >= 0 && c.holdItem < q.total) k_hold_item<<<1, 1, 0, c.stream>>>(c.dep + c.holdItem);
   }
   int dev = 0, nsm = 0;
   UMT_CUDA(cudaGetDevice(&dev));

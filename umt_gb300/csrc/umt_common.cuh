@@ -77,6 +77,7 @@ struct Ctx {
   bool usePDL = true;                           // stage launches as programmatic dependents
   int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
   int *ticket = nullptr;                        // persistent-mode work ticket
+  int holdItem = -1;                            // umt103_hold_item: item given an unsatisfiable dependency
   Schedule sch;
   // materials and sources
   double *Sigt = nullptr, *SigS = nullptr;      // [nz][G]
