@@ -102,3 +102,62 @@ def test_sharded_source_iteration_matches_single_rank():
     assert np.array_equal(res[0][0], res[1][0])
     assert res[0][1] == ref_it and res[0][2]
     assert float(np.max(np.abs(res[0][0] - ref_phi)) / np.max(np.abs(ref_phi))) < 1e-12
+
+
+class FailingSweeper(OracleSweeper):
+    """Raises on its n-th sweep: a rank failure made on the host."""
+
+    def __init__(self, prob, dirs, fail_at):
+        super().__init__(prob, dirs)
+        self.calls, self.fail_at = 0, fail_at
+
+    def sweep(self, STotal, savePsi=False):
+        self.calls += 1
+        if self.fail_at and self.calls == self.fail_at:
+            raise RuntimeError("rank failure injected")
+        return super().sweep(STotal, savePsi)
+
+
+def _rank_fail_main(rank, world, port, out):
+    import datetime
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=10))
+    try:
+        prob = _problem()
+        dirs = sharding.direction_shards(len(prob.weight), world)[rank]
+        sw = FailingSweeper(prob, dirs, fail_at=3 if rank == 1 else 0)
+        try:
+            sharding.source_iterate(sw, prob, sharding.torch_allreduce(), q_ext=prob.q_ext, rel_tol=1e-10,
+                                    max_iters=300)
+            out.put((rank, "finished", sw.calls))
+        except Exception as e:  # the failure this test makes, or the peer's report of it
+            out.put((rank, f"{type(e).__name__}: {e}"[:300], sw.calls))
+    finally:
+        try:
+            dist.destroy_process_group()
+        except Exception:
+            pass
+
+
+def test_rank_failure_ends_the_other_ranks_collective():
+    """One rank raises in its third sweep and leaves; the other rank's next
+    all-reduce ends with an error (peer gone or the process group's 10 s
+    timeout) instead of waiting forever, and both processes exit."""
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_fail_main, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in procs:
+        r, msg, calls = out.get(timeout=120)
+        res[r] = (msg, calls)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode is not None
+    assert res[1][0].startswith("RuntimeError: rank failure injected")
+    assert res[0][0] != "finished"                   # the survivor learned of the failure
+    assert res[0][1] == 3                            # in the iteration the failing rank left
