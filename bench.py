@@ -10,11 +10,15 @@ ratio uniform on [0, 0.5], isotropic source 1.0, vacuum boundaries, seeded
 stand in for the reference's problem; there is no dataset.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--tiles T] [--precision fp32|fp64] [--config 2|3] [--rz]
+                    [--tiles T] [--precision fp32|fp64] [--config 2|3|5] [--rz]
 
 --config 3 is the larger scattering problem: 30^3 tiles, four materials by
 tile (seed 3), total opacity log-uniform on [1e-3, 1e3], scattering ratio up
-to 0.9.  --rz times the 2-D RZ sweep instead (200 x 200 quadrilaterals, 144
+to 0.9.  --config 5 is the strongly scattering 32-group problem: 20^3 tiles,
+total opacity log-uniform on [1, 1e3] per zone and group (seed 5), scattering
+ratio uniform on [0.95, 0.999]; its sweep is timed, without the
+time-to-converge run (plain source iteration needs hundreds of iterations at
+these ratios).  --rz times the 2-D RZ sweep instead (200 x 200 quadrilaterals, 144
 directions, 16 groups).
 
 Multi-GPU: the sweep of one problem does not shard here, so N GPUs run N
@@ -127,14 +131,19 @@ def dist_setup():
 
 
 MATERIALS = {2: "sigma_t log-uniform on [1e-2, 1e2] per zone and group (seed 2), c ~ U[0, 0.5]",
-             3: "4 materials by tile (seed 3), sigma_t log-uniform on [1e-3, 1e3], c ~ U[0, 0.9]"}
+             3: "4 materials by tile (seed 3), sigma_t log-uniform on [1e-3, 1e3], c ~ U[0, 0.9]",
+             5: "sigma_t log-uniform on [1, 1e3] per zone and group (seed 5), c ~ U[0.95, 0.999]"}
 
 
 def make_problem(tiles, config=2):
-    """The scattering workloads: 128 directions (P = Az = 4), 16 groups, q = 1,
-    tau = 1/(c dt) with dt = 1e-3; config 2 draws opacities per zone, config 3
-    per material with a per-tile material index."""
+    """The scattering workloads: 128 directions (P = Az = 4), q = 1,
+    tau = 1/(c dt) with dt = 1e-3; config 2 (16 groups) draws opacities per
+    zone, config 3 (16 groups) per material with a per-tile material index,
+    config 5 (32 groups) per zone with scattering ratios near 1."""
     from umt_gb300.problems import synthetic_problem
+    if config == 5:
+        return synthetic_problem((tiles,) * 3, 4, 4, 32, seed=5, sigt_range=(1.0, 1e3), c_range=(0.95, 0.999),
+                                 q=1.0, time_dependent=True)
     if config == 3:
         return synthetic_problem((tiles,) * 3, 4, 4, 16, seed=3, sigt_range=(1e-3, 1e3), c_range=(0.0, 0.9),
                                  q=1.0, n_materials=4, time_dependent=True)
@@ -180,7 +189,7 @@ def run_reference(args, world, rank):
     line = {"metric": METRIC, "value": v, "unit": "ns", "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"multigroup scattering, {args.tiles}^3 tiles, 128 directions, 16 groups",
+            "config": {"workload": f"multigroup scattering, {args.tiles}^3 tiles, {A} directions, {G} groups",
                        "materials": MATERIALS[args.config], "tiles": args.tiles, "directions": A, "groups": G, "zones": m.nzones,
                        "corners": m.ncornr, "sample_directions": int(sample_angles)},
             "cpu_baseline": {"value": v, "unit": "ns", "cores": nth, "kind": "port",
@@ -323,8 +332,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--tiles", type=int, default=None, help="tiles per axis (default 20, or 30 for --config 3)")
-    ap.add_argument("--config", type=int, default=2, choices=(2, 3),
-                    help="2: opacities per zone (default); 3: four materials by tile, c up to 0.9")
+    ap.add_argument("--config", type=int, default=2, choices=(2, 3, 5),
+                    help="2: opacities per zone (default); 3: four materials by tile, c up to 0.9; "
+                         "5: 32 groups, c in [0.95, 0.999] (no time-to-converge run)")
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
@@ -335,6 +345,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.tiles is None:
         args.tiles = 30 if args.config == 3 else 20
+    if args.config == 5:
+        args.no_ttc = True
     world, rank, local = dist_setup()
     if args.rz:
         if rank == 0:
@@ -442,7 +454,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if prec == capi.UMT_FP32 else "f64", "data": "synthetic",
         "config": {"workload": f"multigroup scattering sweep, {args.tiles}^3 tiles (24-zone tile), "
-                               f"128 directions, 16 groups",
+                               f"{A} directions, {G} groups",
                    "materials": MATERIALS[args.config],
                    "tiles": args.tiles, "zones": m.nzones, "corners": m.ncornr, "directions": A,
                    "groups": G, "units_per_step": units, "parallelism": f"replicas{world}",
