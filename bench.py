@@ -59,11 +59,12 @@ def b_alg(G: int, A: int, s_psi: int, s_g: int, ncf: int = 3) -> float:
 
 
 # DRAM bytes (read + write) per corner*angle*group unit of the FP32 stage
-# kernels, summed over every stage launch of one whole sweep by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum with --cache-control none,
-# 12^3 tiles, 128 directions, 16 groups; the ncu summary is kept under
-# profiles/); scaled by the units of the measured sweep.
-TRAFFIC_B_PER_UNIT_FP32_G16 = 14.166
+# kernels, summed by ncu over every stage launch of one whole sweep of the
+# bench workload itself (dram__bytes_read.sum + dram__bytes_write.sum, one
+# pass, --cache-control none; the ncu summary is kept under profiles/), keyed
+# by (tiles per axis, groups).  Traffic per unit grows with the mesh (13.1 B
+# on 12^3 tiles at 16 groups), so it is reported only where it was measured.
+TRAFFIC_B_PER_UNIT_FP32 = {(20, 16): 17.353, (20, 32): 15.749}
 
 
 def peaks():
@@ -448,7 +449,8 @@ def main():
     k_avg = sum(kern_ms) / len(kern_ms)
     peak, src = peaks()
     achieved = balg * units / (k_avg * 1e-3) / 1e9
-    traffic = TRAFFIC_B_PER_UNIT_FP32_G16 * units if (s == 4 and G == 16) else None
+    tpu = TRAFFIC_B_PER_UNIT_FP32.get((args.tiles, G)) if s == 4 else None
+    traffic = tpu * units if tpu else None
     line = {
         "metric": METRIC, "value": value, "unit": "ns", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_step, "higher_is_better": False, "scaling": "weak",

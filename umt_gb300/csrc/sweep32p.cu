@@ -119,14 +119,16 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   float *psiBA = p.psiB + (size_t)a * p.nb * G + g0;
   // ---- round trip 2: program, previous flux, source, cross sections ----
   {
+    // the program and the previous flux are read once per sweep: evict-first
+    const unsigned long long once = l2_evict_first_policy();
     const uint4 *src = p.prog + h.z;
-    for (int e = lane; e < nch; e += GT) cp_async16_cg(sB + 16 * e, src + e);
+    for (int e = lane; e < nch; e += GT) cp_async16_cg_pol(sB + 16 * e, src + e, once);
     const float *po = p.psi_old + (abase + c0) * G + g0;
     const float *st = p.STotal + (size_t)c0 * G + g0;
 #pragma unroll
     for (int c = 0; c < UMT_MAXCORNER; ++c)
       if (c < nC) {
-        cp_async(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4);
+        cp_async_pol(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4, once);
         cp_async(sS + c * RP + g0, st + (size_t)c * G, GPL * 4);
       }
   }
