@@ -22,11 +22,6 @@ __device__ __forceinline__ void cp_async(void *smem, const void *gmem, int bytes
   else
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
 }
-// 16-byte copy that bypasses L1 (streamed data read once per block).
-__device__ __forceinline__ void cp_async16_cg(void *smem, const void *gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
 // An L2 cache policy under which the lines a copy brings in are the first to
 // be evicted: for data a sweep reads exactly once (the previous flux, the zone
 // programs), so that it does not push out of L2 the rows that later work
@@ -36,7 +31,8 @@ __device__ __forceinline__ unsigned long long l2_evict_first_policy() {
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
   return pol;
 }
-// cp_async / cp_async16_cg with an L2 cache policy.
+// cp_async with an L2 cache policy; the 16-byte .cg form also bypasses L1
+// (for data read once per block).
 __device__ __forceinline__ void cp_async_pol(void *smem, const void *gmem, int bytes, unsigned long long pol) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   if (bytes == 16)
