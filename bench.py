@@ -65,7 +65,7 @@ def b_alg(G: int, A: int, s_psi: int, s_g: int, ncf: int = 3) -> float:
 # pass, --cache-control none; the ncu summary is kept under profiles/), keyed
 # by (tiles per axis, groups).  Traffic per unit grows with the mesh (13.1 B
 # on 12^3 tiles at 16 groups), so it is reported only where it was measured.
-TRAFFIC_B_PER_UNIT_FP32 = {(20, 16): 17.353, (20, 32): 15.749}
+TRAFFIC_B_PER_UNIT_FP32 = {(20, 16): 17.353, (20, 32): 15.749, (30, 16): 19.649}
 
 
 def peaks():
