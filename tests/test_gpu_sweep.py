@@ -103,6 +103,33 @@ def test_fp32_group_tiles(umtlib, G, tile, mode):
     assert rel_err(PsiB, ref["PsiB"]) < 1e-4
 
 
+@pytest.mark.parametrize("mode", [0, 2])
+def test_fp32_thick_strongly_scattering_32_groups(umtlib, mode):
+    """The 32-group, strongly scattering workload's distribution (sigma_t
+    log-uniform on [1, 1e3], c in [0.95, 0.999], 128 directions) on 3^3
+    tiles: optically thick zones, where the FP32 EZ closure works near its
+    cap, agree with the oracle, in the max norm and corner by corner."""
+    prob = synthetic_problem((3, 3, 3), 4, 4, 32, seed=5, sigt_range=(1.0, 1e3), c_range=(0.95, 0.999),
+                             q=1.0, time_dependent=True)
+    m = prob.mesh
+    rng = np.random.default_rng(55)
+    phi = rng.uniform(0.5, 2.0, size=(m.ncornr, prob.ngr))
+    STotal = (prob.sigs[m.cToZone] * phi + prob.q_ext[m.cToZone]) / (4 * np.pi)
+    ref = oracle_sweep(prob, STotal=STotal, Psi=prob.psi0)
+    umtlib.init(m, prob.omega, prob.weight, prob.ngr)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    umtlib.set_sweep_mode(mode)
+    PsiB = np.zeros((len(prob.weight), m.nbelem, prob.ngr))
+    Phi = umtlib.sweep(STotal, savePsi=True, PsiB=PsiB, precision=capi.UMT_FP32)
+    Psi, _ = umtlib.get_psi(capi.UMT_FP32)
+    assert rel_err(Phi, ref["Phi"]) < 1e-5
+    assert rel_err(Psi, ref["Psi"]) < 1e-4
+    assert rel_err(PsiB, ref["PsiB"]) < 1e-4
+    big = ref["Phi"] > 1e-3 * ref["Phi"].max()
+    assert np.max(np.abs(Phi[big] / ref["Phi"][big] - 1.0)) < 1e-4
+
+
 @pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_fp32_sweep_modes(umtlib, mode):
     """Per-stage launches of the zone-program (0), corner-slot (2) and
