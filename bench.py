@@ -10,7 +10,7 @@ ratio uniform on [0, 0.5], isotropic source 1.0, vacuum boundaries, seeded
 stand in for the reference's problem; there is no dataset.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--tiles T] [--precision fp32|fp64] [--config 2|3|5] [--rz]
+                    [--tiles T] [--precision fp32|fp64] [--config 2|3|4|5] [--rz]
 
 --config 3 is the larger scattering problem: 30^3 tiles, four materials by
 tile (seed 3), total opacity log-uniform on [1e-3, 1e3], scattering ratio up
@@ -19,7 +19,10 @@ flux buffers (2 x 78 GB) would not fit beside the FP32 ones.  --config 5 is the 
 total opacity log-uniform on [1, 1e3] per zone and group (seed 5), scattering
 ratio uniform on [0.95, 0.999]; its sweep is timed, without the
 time-to-converge run (plain source iteration needs hundreds of iterations at
-these ratios).  --rz times the 2-D RZ sweep instead (200 x 200 quadrilaterals, 144
+these ratios).  --config 4 sweeps a batch of independent problems of uneven
+size from one graph launch (tiles per axis U{4..16}, 4 to 64 groups, 32 or
+128 directions; seed 4), the draws that fit in --c4-budget GB of device
+memory, against the same contexts swept one after another.  --rz times the 2-D RZ sweep instead (200 x 200 quadrilaterals, 144
 directions, 16 groups).
 
 Multi-GPU: the sweep of one problem does not shard here, so N GPUs run N
@@ -327,6 +330,103 @@ def run_rz(args):
     print(json.dumps(line), flush=True)
 
 
+def config4_draws(n=64, seed=4):
+    """The batched workload's problems: tiles per axis U{4..16}, P = Az in
+    {2, 4} (32 or 128 directions), G in {4, 8, 16, 32, 64}."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        t = int(rng.integers(4, 17))
+        out.append((t, int(rng.choice([2, 4])), int(rng.choice([4, 8, 16, 32, 64])), 400 + k))
+    return out
+
+
+def config4_device_bytes(t, P, G):
+    """Device bytes of one FP32 context, estimated with a 10% margin: flux
+    (two buffers), corner records, zone programs and headers, FP64
+    projections; 7.33 corners per zone."""
+    A, nz = 8 * P * P, 24 * t ** 3
+    nc = nz * 22 / 3
+    return 1.1 * (2 * nc * A * G * 4 + 32 * A * nc + 371 * A * nz + 48 * A * nc)
+
+
+def run_config4(args):
+    """Config 4: independent problems of uneven size resident in separate
+    contexts, swept from one graph launch (umt103_batch_sweep), against the
+    same contexts swept one after another.  The 64 draws hold about 430 GB in
+    FP32, more than one GPU, so the draws are taken in order while their
+    estimated device memory stays within --c4-budget GB; each problem's host
+    arrays are freed once its context holds them."""
+    import gc
+    from umt_gb300 import build, capi
+    from umt_gb300.problems import synthetic_problem
+    build.build()
+    lib = capi.Library()
+    draws = config4_draws()
+    taken, used = [], 0.0
+    for d in draws:
+        est = config4_device_bytes(*d[:3])
+        if used + est > args.c4_budget * 1e9:
+            break
+        taken.append(d); used += est
+    ids, units, balg_units = [], 0, 0.0
+    for (t, P, G, seed) in taken:
+        pr = synthetic_problem((t,) * 3, P, P, G, seed=seed, time_dependent=True)
+        cid = lib.context_create()
+        lib.context_select(cid)
+        lib.init(pr.mesh, pr.omega, pr.weight, G, flags=2 | 8)
+        lib.set_materials(pr.sigt, pr.sigs, pr.tau)
+        lib.set_psi(pr.psi0, None)
+        lib.set_source(np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi))
+        u = pr.mesh.ncornr * len(pr.weight) * G
+        units += u
+        balg_units += b_alg(G, len(pr.weight), 4, 4) * u
+        ids.append(cid)
+        del pr
+        gc.collect()
+    lib.context_select(0)
+    for _ in range(args.warmup):
+        lib.batch_sweep(ids, capi.UMT_FP32)
+    for cid in ids:
+        lib.context_select(cid)
+        for _ in range(args.warmup):
+            lib.sweep_resident(False, capi.UMT_FP32)
+    lib.context_select(0)
+    with ClockSampler(0) as clk:
+        batch_ms = [lib.batch_sweep(ids, capi.UMT_FP32) for _ in range(args.steps)]
+        seq_ms = []
+        for _ in range(args.steps):
+            tot = 0.0
+            for cid in ids:
+                lib.context_select(cid)
+                lib.sweep_resident(False, capi.UMT_FP32)
+                tot += lib.timing()[0]
+            seq_ms.append(tot)
+    lib.context_select(0)
+    for cid in ids:
+        lib.context_destroy(cid)
+    t_b = statistics.median(batch_ms)
+    t_s = statistics.median(seq_ms)
+    peak, src = peaks()
+    achieved = balg_units / (t_b * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": t_b * 1e6 / units, "unit": "ns", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_b, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batch of independent problems (tiles per axis U{4..16}, G in {4..64}, "
+                                   "32 or 128 directions; seed 4), one graph launch",
+                       "problems": len(taken), "of_draws": len(draws), "device_budget_gb": args.c4_budget,
+                       "draws": [list(d[:3]) for d in taken], "units_per_step": units,
+                       "l2": "inputs larger than L2"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": src,
+                         "kernel": "whole batch (stage kernels and tallies of every problem)",
+                         "bytes_per_unit": balg_units / units},
+            "sequential": {"value": t_s * 1e6 / units, "unit": "ns", "ms_per_step": t_s,
+                           "how": "the same contexts swept one after another (umt103_sweep_resident)"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,7 +434,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--tiles", type=int, default=None, help="tiles per axis (default 20, or 30 for --config 3)")
-    ap.add_argument("--config", type=int, default=2, choices=(2, 3, 5),
+    ap.add_argument("--c4-budget", type=float, default=160.0,
+                    help="--config 4: device memory (GB) the batch of draws may take")
+    ap.add_argument("--config", type=int, default=2, choices=(2, 3, 4, 5),
                     help="2: opacities per zone (default); 3: four materials by tile, c up to 0.9; "
                          "5: 32 groups, c in [0.95, 0.999] (3 and 5: no time-to-converge run)")
     ap.add_argument("--precision", default="fp32")
@@ -350,6 +452,13 @@ def main():
     if args.config in (3, 5):
         args.no_ttc = True
     world, rank, local = dist_setup()
+    if args.config == 4:
+        if rank == 0:
+            if args.impl == "reference":
+                print(json.dumps({"impl": "reference", "unavailable": "config 4 is timed on the GPU arm only"}))
+            else:
+                run_config4(args)
+        return
     if args.rz:
         if rank == 0:
             run_rz(args)
