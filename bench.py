@@ -330,13 +330,13 @@ def run_rz(args):
     print(json.dumps(line), flush=True)
 
 
-def config4_draws(n=64, seed=4):
-    """The batched workload's problems: tiles per axis U{4..16}, P = Az in
-    {2, 4} (32 or 128 directions), G in {4, 8, 16, 32, 64}."""
+def config4_draws(n=64, seed=4, tiles=(4, 16)):
+    """The batched workload's problems: tiles per axis U{4..16} (or the given
+    range), P = Az in {2, 4} (32 or 128 directions), G in {4, 8, 16, 32, 64}."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n):
-        t = int(rng.integers(4, 17))
+        t = int(rng.integers(tiles[0], tiles[1] + 1))
         out.append((t, int(rng.choice([2, 4])), int(rng.choice([4, 8, 16, 32, 64])), 400 + k))
     return out
 
@@ -362,7 +362,7 @@ def run_config4(args):
     from umt_gb300.problems import synthetic_problem
     build.build()
     lib = capi.Library()
-    draws = config4_draws()
+    draws = config4_draws(tiles=tuple(args.c4_tiles))
     taken, used = [], 0.0
     for d in draws:
         est = config4_device_bytes(*d[:3])
@@ -412,8 +412,8 @@ def run_config4(args):
     line = {"metric": METRIC, "value": t_b * 1e6 / units, "unit": "ns", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_b, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batch of independent problems (tiles per axis U{4..16}, G in {4..64}, "
-                                   "32 or 128 directions; seed 4), one graph launch",
+            "config": {"workload": "batch of independent problems (tiles per axis U{%d..%d}, G in {4..64}, "
+                                   "32 or 128 directions; seed 4), one graph launch" % tuple(args.c4_tiles),
                        "problems": len(taken), "of_draws": len(draws), "device_budget_gb": args.c4_budget,
                        "draws": [list(d[:3]) for d in taken], "units_per_step": units,
                        "l2": "inputs larger than L2"},
@@ -436,6 +436,8 @@ def main():
     ap.add_argument("--tiles", type=int, default=None, help="tiles per axis (default 20, or 30 for --config 3)")
     ap.add_argument("--c4-budget", type=float, default=160.0,
                     help="--config 4: device memory (GB) the batch of draws may take")
+    ap.add_argument("--c4-tiles", type=int, nargs=2, default=(4, 16), metavar=("LO", "HI"),
+                    help="--config 4: range of tiles per axis of the draws (default 4 16)")
     ap.add_argument("--config", type=int, default=2, choices=(2, 3, 4, 5),
                     help="2: opacities per zone (default); 3: four materials by tile, c up to 0.9; "
                          "5: 32 groups, c in [0.95, 0.999] (3 and 5: no time-to-converge run)")
