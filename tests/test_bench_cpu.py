@@ -57,3 +57,22 @@ def test_reference_arm_json_line():
     assert d["value"] > 0 and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["groups"] == 16 and d["config"]["directions"] == 128
+
+
+def test_config4_draws_and_memory_budget():
+    """The batched workload's draws have the stated ranges; all 64 need more
+    device memory than one GPU holds, so the bench takes the prefix that fits
+    its budget; the estimate errs high (the 20^3-tile, 128-direction,
+    16-group context holds about 48 GB)."""
+    d = bench.config4_draws()
+    assert len(d) == 64 and d == bench.config4_draws()
+    assert all(4 <= t <= 16 and P in (2, 4) and G in (4, 8, 16, 32, 64) for t, P, G, _ in d)
+    est = [bench.config4_device_bytes(t, P, G) for t, P, G, _ in d]
+    assert sum(est) > 280e9
+    n, used = 0, 0.0
+    while n < len(est) and used + est[n] <= 160e9:
+        used += est[n]; n += 1
+    assert n == 11
+    assert 48e9 < bench.config4_device_bytes(20, 4, 16) < 56e9
+    small = bench.config4_draws(tiles=(2, 4))
+    assert all(2 <= t <= 4 for t, _, _, _ in small)
