@@ -228,6 +228,21 @@ def cpu_baseline_sample(prob, budget_s=20.0):
             "sample": f"{n_ang} of {len(prob.weight)} directions on the full mesh, all groups, FP64"}
 
 
+def fp64_sweep_figure(lib, prob, units, steps=3):
+    """The same workload swept with the FP64 flux (the parity path, FP64
+    arithmetic throughout): device time per sweep, so the FP32 figure has a
+    same-precision companion beside the FP64 CPU arm."""
+    from umt_gb300 import capi
+    lib.sweep_resident(False, capi.UMT_FP64)
+    ms = []
+    for _ in range(steps):
+        lib.sweep_resident(False, capi.UMT_FP64)
+        ms.append(lib.timing()[0])
+    t = statistics.median(ms)
+    return {"value": t * 1e6 / units, "unit": "ns", "ms_per_step": t, "steps": steps, "dtype": "f64",
+            "kernel": "k_sweep<double> (all dependency stages) + FP64 tally", "bound": "fp64 pipe"}
+
+
 def time_to_converge(lib, prob, use_gta=False, tol64=1e-8, tol32=1e-7):
     """Second half of the metric: wall time of source iteration to convergence,
     plain FP64 GPU sweeps versus the FP32 sweep (FP64 tallies), and the FP32
@@ -393,20 +408,27 @@ def run_config4(args):
             lib.sweep_resident(False, capi.UMT_FP32)
     lib.context_select(0)
     with ClockSampler(0) as clk:
-        batch_ms = [lib.batch_sweep(ids, capi.UMT_FP32) for _ in range(args.steps)]
-        seq_ms = []
+        batch_ms, batch_wall = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            batch_ms.append(lib.batch_sweep(ids, capi.UMT_FP32))
+            batch_wall.append((time.perf_counter() - t0) * 1e3)
+        seq_ms, seq_wall = [], []
         for _ in range(args.steps):
             tot = 0.0
+            t0 = time.perf_counter()
             for cid in ids:
                 lib.context_select(cid)
                 lib.sweep_resident(False, capi.UMT_FP32)
                 tot += lib.timing()[0]
+            seq_wall.append((time.perf_counter() - t0) * 1e3)
             seq_ms.append(tot)
     lib.context_select(0)
     for cid in ids:
         lib.context_destroy(cid)
     t_b = statistics.median(batch_ms)
     t_s = statistics.median(seq_ms)
+    w_b, w_s = statistics.median(batch_wall), statistics.median(seq_wall)
     peak, src = peaks()
     achieved = balg_units / (t_b * 1e-3) / 1e9
     line = {"metric": METRIC, "value": t_b * 1e6 / units, "unit": "ns", "n_gpus": 1, "steps": args.steps,
@@ -423,6 +445,9 @@ def run_config4(args):
                          "bytes_per_unit": balg_units / units},
             "sequential": {"value": t_s * 1e6 / units, "unit": "ns", "ms_per_step": t_s,
                            "how": "the same contexts swept one after another (umt103_sweep_resident)"},
+            "wall_clock": {"batch_ms": w_b, "sequential_ms": w_s, "ratio": w_s / w_b,
+                           "how": "host time of each whole call (launch, wait, status checks); the batch "
+                                  "graph is instantiated once and replayed (kept by umt103_batch_sweep)"},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -444,6 +469,7 @@ def main():
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 same-workload sweep figure")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
     ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (precision as --precision)")
     ap.add_argument("--rz-cells", type=int, default=200, help="RZ mesh: cells per direction")
@@ -484,7 +510,10 @@ def main():
     prob = make_problem(args.tiles, args.config)
     m = prob.mesh
     A, G = len(prob.weight), prob.ngr
-    lib.init(m, prob.omega, prob.weight, G, flags=3 if world == 1 and not args.no_ttc else
+    # the FP64 flux too (same-precision figure and time to converge) where it fits beside the FP32 one
+    # (config 2 unless --no-ttc, config 5 unless --no-fp64; config 3's FP64 flux would not fit)
+    fp64_ok = world == 1 and not args.no_fp64 and ((args.config == 2 and not args.no_ttc) or args.config == 5)
+    lib.init(m, prob.omega, prob.weight, G, flags=3 if (fp64_ok or (world == 1 and not args.no_ttc)) else
              (2 if prec == capi.UMT_FP32 else 1))
     lib.set_materials(prob.sigt, prob.sigs, prob.tau)
     lib.set_psi(prob.psi0, None)
@@ -591,6 +620,8 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
     }
+    if world == 1 and prec == capi.UMT_FP32 and fp64_ok:
+        line["fp64"] = fp64_sweep_figure(lib, prob, units)
     if world == 1 and not args.no_ttc:
         line["time_to_converge"] = time_to_converge(lib, prob, use_gta=args.gta)
     if not args.no_cpu_baseline and world == 1:

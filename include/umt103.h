@@ -103,7 +103,15 @@ int umt103_context_destroy(int id);   /* id > 0; releases its buffers */
  * contexts' captured sweeps become independent child graphs, so problems of
  * different zone, group and direction counts run concurrently.  *ms (may be
  * NULL) receives the device time of the whole batch.  Each context's
- * PhiTotal is left on its device (umt103_get_phi after selecting it).
+ * PhiTotal is left on its device (umt103_get_phi after selecting it).  The
+ * instantiated batch graph is kept for the same list, precision and buffer
+ * parities until a listed context changes (materials, group tile, sweep
+ * mode, re-initialisation), so a repeated batch costs one graph launch.
+ * Every listed context's device status word is read and cleared after the
+ * launch; a bounds or timeout flag returns UMT_ERR_BOUNDS / UMT_ERR_TIMEOUT
+ * naming the context.  A context with a held work item (umt103_hold_item) or
+ * an RZ problem is refused with UMT_ERR_STATE; a context listed twice with
+ * UMT_ERR_ARG.
  */
 int umt103_batch_sweep(const int *ids, int n, int precision, double *ms);
 
@@ -208,8 +216,11 @@ int umt103_tally_precision(const double *siga, double speed_light, int precision
  * calls give bit-identical results.  The scratch need not start at zero:
  * each call writes every value it later reads.  Limit: max(ncornr*G, nangles*nbelem)
  * must not exceed UMT_NOALLOC_MAX_BLOCKS*4096 elements (UMT_ERR_ARG with a
- * message otherwise).  The first call on a device looks up the scratch
- * address on that device; make that first call before any stream capture.
+ * message otherwise).  Every call looks up the scratch address on the
+ * current device (a lookup, not an allocation), so a primary context that
+ * was reset and recreated is followed; make the first call on a device
+ * before any stream capture, because that lookup may load the library's
+ * device image.  An RZ context is refused (UMT_ERR_STATE).
  * All calls share the scratch: calls that overlap on the GPU (other threads,
  * other streams of the same device) race and must be serialised by the caller.
  */
@@ -294,17 +305,19 @@ int umt103_last_timing(double *out3);
  * (gpu/GPU_SweepUCBxyz.cu:30-31). */
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane);
 
-/* FP32 sweep kernel and scheduling.  Modes 0, 2 and 3 launch one kernel per
+/* FP32 sweep kernel and scheduling.  Modes 0 and 2 launch one kernel per
  * dependency stage (the hyperplane loop of snac/SweepUCBxyz.F90:103, all
  * directions at once):
  *   0 (default) zone-program kernel: each (direction, zone) pair runs a
  *     compact list of its face operations built once on the device (group
- *     tiles with 2 or 4 groups per lane; other tiles fall back to mode 2);
- *   2 unrolled corner-slot kernel;
- *   3 compact face-list kernel (corner-face slots classified per sweep);
+ *     tiles with 2 or 4 groups per lane; other tiles, and geometry the
+ *     program format cannot hold, fall back to mode 2);
+ *   2 unrolled corner-slot kernel (every group tile; the fallback);
  *   1 one persistent launch in which each (direction, zone) pair starts as
  *     soon as its upwind zones have finished (bounded waits; a wait that
- *     gives up makes the sweep return UMT_ERR_TIMEOUT). */
+ *     gives up makes the sweep return UMT_ERR_TIMEOUT).  Slower than mode 0;
+ *     kept as the one kernel whose blocks wait on one another, which the
+ *     bounded-wait failure path (umt103_hold_item) exercises. */
 int umt103_set_sweep_mode(int mode);
 
 /* Number of kernels one sweep of the given precision launches (>= 0). */

@@ -17,7 +17,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF = os.environ.get("UMT_REFERENCE", "/root/reference")
+# The UMT source tree: $UMT_REFERENCE, else a directory named "reference"
+# beside this repository's checkout (absent on the GPU hosts).
+REF = os.environ.get("UMT_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def build(force=False):

@@ -190,6 +190,13 @@ def test_rz_precision_refusals(umtlib):
     with pytest.raises(capi.UmtError) as e:              # the 3-D sweep refuses an RZ context
         umtlib.sweep(STotal, precision=capi.UMT_FP32)
     assert e.value.code == capi.UMT_ERR_STATE
+    # the 3-D energy edits (3-D boundary projections) refuse an RZ context too
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.tally(None, precision=capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_STATE
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.tally_noalloc(None, precision=capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_STATE
 
 
 def test_rz_errors(umtlib):

@@ -130,11 +130,10 @@ def test_fp32_thick_strongly_scattering_32_groups(umtlib, mode):
     assert np.max(np.abs(Phi[big] / ref["Phi"][big] - 1.0)) < 1e-4
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2, 3])
+@pytest.mark.parametrize("mode", [0, 1, 2])
 def test_fp32_sweep_modes(umtlib, mode):
-    """Per-stage launches of the zone-program (0), corner-slot (2) and
-    compact face-list (3) kernels, and the persistent dependency-driven
-    launch (1)."""
+    """Per-stage launches of the zone-program (0) and corner-slot (2)
+    kernels, and the persistent dependency-driven launch (1)."""
     prob = synthetic_problem((3, 2, 2), 4, 4, 16, seed=6, time_dependent=True)
     m = prob.mesh
     STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
@@ -187,13 +186,39 @@ def test_batch_of_contexts_matches_single_runs(umtlib, specs):
         umtlib.set_source(np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi))
         ids.append(cid)
     umtlib.context_select(0)
-    ms = umtlib.batch_sweep(ids, capi.UMT_FP32)
-    assert ms > 0
-    for cid, pr, ref in zip(ids, probs, single):
-        umtlib.context_select(cid)
-        phi = umtlib.get_phi(pr.mesh.ncornr, pr.ngr)
-        assert np.array_equal(phi, ref)
+    for _ in range(2):                       # the second launch replays the kept batch graph
+        ms = umtlib.batch_sweep(ids, capi.UMT_FP32)
+        assert ms > 0
+        for cid, pr, ref in zip(ids, probs, single):
+            umtlib.context_select(cid)
+            phi = umtlib.get_phi(pr.mesh.ncornr, pr.ngr)
+            assert np.array_equal(phi, ref)
+        umtlib.context_select(0)
+    # a changed context (new materials) is captured again, not replayed stale
+    pr = probs[0]
+    umtlib.context_select(ids[0])
+    umtlib.set_materials(2.0 * pr.sigt, pr.sigs, pr.tau)
+    st = np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi)
+    want = umtlib.sweep(st, precision=capi.UMT_FP32)
     umtlib.context_select(0)
+    umtlib.batch_sweep(ids, capi.UMT_FP32)
+    umtlib.context_select(ids[0])
+    assert np.array_equal(umtlib.get_phi(pr.mesh.ncornr, pr.ngr), want)
+    # refused: a context listed twice, a context with a held work item
+    umtlib.context_select(0)
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.batch_sweep([ids[0], ids[0]], capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_ARG
+    umtlib.context_select(ids[-1])
+    umtlib.hold_item(0)
+    umtlib.context_select(0)
+    with pytest.raises(capi.UmtError) as e:
+        umtlib.batch_sweep(ids, capi.UMT_FP32)
+    assert e.value.code == capi.UMT_ERR_STATE
+    umtlib.context_select(ids[-1])
+    umtlib.hold_item(-1)
+    umtlib.context_select(0)
+    umtlib.batch_sweep(ids, capi.UMT_FP32)
     for cid in ids:
         umtlib.context_destroy(cid)
 

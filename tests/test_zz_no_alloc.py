@@ -48,3 +48,32 @@ def test_tally_noalloc_matches_allocating_entry_point(umtlib, precision):
     none = umtlib.tally_noalloc(None, precision=precision)
     assert none["PowerAbsorbed"] == 0.0
     assert none["EnergyRadiation"] == first["EnergyRadiation"]
+
+
+def test_tally_noalloc_with_device_memory_reserved(umtlib):
+    """A caller that has already reserved (almost) all free device memory --
+    the situation of a host code whose pool owns the device heap -- can still
+    take the energy edits: with one tensor holding all but 64 MiB of free
+    memory, the call succeeds and matches the same call made before."""
+    torch = pytest.importorskip("torch")
+    prob = synthetic_problem((2, 2, 2), 2, 2, 4, seed=22, time_dependent=True)
+    m = prob.mesh
+    umtlib.init(m, prob.omega, prob.weight, prob.ngr, flags=2 | 8)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    STotal = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    umtlib.sweep(STotal, savePsi=True, precision=capi.UMT_FP32)
+    siga_dev = torch.as_tensor(np.ascontiguousarray(prob.siga), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    before = umtlib.tally_noalloc(siga_dev.data_ptr(), precision=capi.UMT_FP32)
+    free = torch.cuda.mem_get_info()[0]
+    hold = torch.empty(max(free - (64 << 20), 0), dtype=torch.uint8, device="cuda")
+    try:
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] < (256 << 20)        # the device is (nearly) full
+        during = umtlib.tally_noalloc(siga_dev.data_ptr(), precision=capi.UMT_FP32)
+    finally:
+        del hold
+        torch.cuda.empty_cache()
+    for key in ("EnergyRadiation", "PowerEscape", "PowerIncident", "PowerAbsorbed"):
+        assert during[key] == before[key], key

@@ -1,7 +1,7 @@
 """ctypes binding of libumt103.so (include/umt103.h).
 
 This is the Python face of the C-ABI; a Fortran caller binds the same entry
-points through ISO_C_BINDING.  Loading fails loudly when
+points through an ISO_C_BINDING interface block.  Loading fails loudly when
 the library has not been built: there is no fallback path.
 """
 from __future__ import annotations

@@ -140,59 +140,133 @@ int umt103_context_destroy(int id) {
 // One CUDA graph that sweeps several contexts at once: each context's captured
 // sweep graph (source conversion, every dependency stage, tally) becomes an
 // independent child node, so problems of different sizes, group counts and
-// direction counts run concurrently from a single launch.
+// direction counts run concurrently from a single launch.  The instantiated
+// graph is kept for the same context list, precision, buffer parities and
+// context generations, so a repeated batch costs one launch.
+struct BatchGraph {
+  std::vector<int> ids, curs;
+  std::vector<unsigned long long> gens;
+  int precision = -1;
+  cudaGraphExec_t exec = nullptr;
+};
+static std::vector<BatchGraph> g_batch;          // most recently used last
+constexpr size_t kBatchGraphsKept = 8;
+
+static void drop_batch_graph(size_t k) {
+  if (g_batch[k].exec) cudaGraphExecDestroy(g_batch[k].exec);
+  g_batch.erase(g_batch.begin() + (long)k);
+}
+
 int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
   if (!ids || n <= 0) return set_error(UMT_ERR_ARG, "empty batch");
   if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
-  Ctx *keep = g_cur;
-  std::vector<cudaGraph_t> children;
-  int rc = 0;
-  for (int k = 0; k < n && !rc; ++k) {
+  BatchGraph key;
+  key.precision = precision;
+  for (int k = 0; k < n; ++k) {
     const int id = ids[k];
-    if (id < 0 || id >= (int)g_ctx.size() || !g_ctx[id] || !g_ctx[id]->ready) {
-      rc = set_error(UMT_ERR_ARG, "batch: context %d not initialised", id);
-      break;
-    }
-    if (g_ctx[id]->rz) {
-      rc = set_error(UMT_ERR_STATE, "batch: context %d holds an RZ problem (umt103_sweep_rz)", id);
-      break;
-    }
-    g_cur = g_ctx[id];
-    cudaGraph_t gr = nullptr;
-    rc = capture_sweep_graph(*g_cur, precision, &gr);
-    if (!rc) children.push_back(gr);
+    if (id < 0 || id >= (int)g_ctx.size() || !g_ctx[id] || !g_ctx[id]->ready)
+      return set_error(UMT_ERR_ARG, "batch: context %d not initialised", id);
+    for (int j = 0; j < k; ++j)
+      if (ids[j] == id) return set_error(UMT_ERR_ARG, "batch: context %d listed twice", id);
+    Ctx &c = *g_ctx[id];
+    if (c.rz) return set_error(UMT_ERR_STATE, "batch: context %d holds an RZ problem (umt103_sweep_rz)", id);
+    if (c.holdItem >= 0)
+      return set_error(UMT_ERR_STATE, "batch: context %d has a held work item (umt103_hold_item); sweep it alone", id);
+    if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "batch: context %d has no FP64 flux", id);
+    if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "batch: context %d has no FP32 flux", id);
+    key.ids.push_back(id);
+  }
+  Ctx *keep = g_cur;
+  int rc = 0;
+  // one-time preparation of each context (outside any capture), then the key
+  for (int k = 0; k < n && !rc; ++k) {
+    g_cur = g_ctx[ids[k]];
+    bool prog = false;
+    if (precision == UMT_FP32) rc = fp32_program_path(*g_cur, &prog);
   }
   g_cur = keep;
-  cudaGraph_t parent = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  cudaStream_t st = g_ctx[ids[0]] ? g_ctx[ids[0]]->stream : nullptr;
-  if (!rc) {
-    cudaError_t e = cudaGraphCreate(&parent, 0);
-    for (size_t k = 0; k < children.size() && e == cudaSuccess; ++k) {
-      cudaGraphNode_t node;
-      e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, children[k]);
-    }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, parent, 0);
-    if (e == cudaSuccess) e = cudaEventCreate(&e0);
-    if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
-    if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
-    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess && ms) {
-      float f = 0.f;
-      e = cudaEventElapsedTime(&f, e0, e1);
-      *ms = f;
-    }
-    if (e != cudaSuccess) rc = set_error(UMT_ERR_CUDA, "batch sweep: %s", cudaGetErrorString(e));
+  if (rc) return rc;
+  for (int k = 0; k < n; ++k) {
+    const Ctx &c = *g_ctx[ids[k]];
+    key.curs.push_back(precision == UMT_FP64 ? c.cur64 : c.cur32);
+    key.gens.push_back(c.graphGen);
   }
-  if (e0) cudaEventDestroy(e0);
-  if (e1) cudaEventDestroy(e1);
-  if (exec) cudaGraphExecDestroy(exec);
-  if (parent) cudaGraphDestroy(parent);
-  for (auto gr : children) cudaGraphDestroy(gr);
-  return rc;
+  cudaGraphExec_t exec = nullptr;
+  for (size_t k = 0; k < g_batch.size(); ++k) {
+    const BatchGraph &b = g_batch[k];
+    if (b.precision == key.precision && b.ids == key.ids && b.curs == key.curs && b.gens == key.gens) {
+      key.exec = b.exec;
+      g_batch.erase(g_batch.begin() + (long)k);
+      exec = key.exec;
+      break;
+    }
+  }
+  if (!exec) {
+    std::vector<cudaGraph_t> children;
+    for (int k = 0; k < n && !rc; ++k) {
+      g_cur = g_ctx[ids[k]];
+      cudaGraph_t gr = nullptr;
+      rc = capture_sweep_graph(*g_cur, precision, &gr);
+      if (!rc) children.push_back(gr);
+    }
+    g_cur = keep;
+    cudaGraph_t parent = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!rc) {
+      e = cudaGraphCreate(&parent, 0);
+      for (size_t k = 0; k < children.size() && e == cudaSuccess; ++k) {
+        cudaGraphNode_t node;
+        e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, children[k]);
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, parent, 0);
+      if (e != cudaSuccess) {
+        exec = nullptr;
+        rc = set_error(UMT_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+      }
+    }
+    if (parent) cudaGraphDestroy(parent);
+    for (auto gr : children) cudaGraphDestroy(gr);
+    if (rc) return rc;
+    key.exec = exec;
+  }
+  // keep the graph (most recent last); entries of stale generations are dropped
+  for (size_t k = 0; k < g_batch.size();) {
+    bool stale = false;
+    for (size_t j = 0; j < g_batch[k].ids.size() && !stale; ++j) {
+      const int id = g_batch[k].ids[j];
+      stale = id >= (int)g_ctx.size() || !g_ctx[id] || g_ctx[id]->graphGen != g_batch[k].gens[j];
+    }
+    if (stale) drop_batch_graph(k); else ++k;
+  }
+  while (g_batch.size() >= kBatchGraphsKept) drop_batch_graph(0);
+  g_batch.push_back(key);
+
+  cudaStream_t st = g_ctx[ids[0]]->stream;
+  cudaEvent_t e0 = g_ctx[ids[0]]->ev0, e1 = g_ctx[ids[0]]->ev1;
+  cudaError_t e = cudaEventRecord(e0, st);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess && ms) {
+    float f = 0.f;
+    e = cudaEventElapsedTime(&f, e0, e1);
+    *ms = f;
+  }
+  if (e != cudaSuccess) return set_error(UMT_ERR_CUDA, "batch sweep: %s", cudaGetErrorString(e));
+  // every context's device status word: read, cleared once reported
+  int bad = 0;
+  for (int k = 0; k < n; ++k) {
+    Ctx &c = *g_ctx[ids[k]];
+    unsigned w = 0;
+    UMT_CUDA(cudaMemcpy(&w, c.status, sizeof(w), cudaMemcpyDeviceToHost));
+    if (!w) continue;
+    UMT_CUDA(cudaMemset(c.status, 0, sizeof(unsigned)));
+    if (!bad) {
+      if (w & UMT_DEV_BOUNDS) bad = set_error(UMT_ERR_BOUNDS, "batch: device bounds check in context %d", ids[k]);
+      else if (w & UMT_DEV_TIMEOUT) bad = set_error(UMT_ERR_TIMEOUT, "batch: device wait timed out in context %d", ids[k]);
+    }
+  }
+  return bad;
 }
 
 static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int flags);
@@ -247,6 +321,7 @@ static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int fla
       return set_error(UMT_ERR_ARG, "zone %d corner range out of bounds", z);
   }
   c.nz = nz; c.nc = nc; c.nb = nb; c.A = A; c.G = G; c.flags = (flags & 3) ? (flags & 3) : 3;
+  invalidate_graphs(c);                                   // a fresh graph generation
   UMT_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
   UMT_CUDA(cudaEventCreate(&c.ev0));
   UMT_CUDA(cudaEventCreate(&c.ev1));
@@ -700,7 +775,7 @@ int umt103_set_gta(int max_krylov, double tol, int spectrum) {
 int umt103_set_sweep_mode(int mode) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
-  if (mode < 0 || mode > 3) return set_error(UMT_ERR_ARG, "sweep mode must be 0, 1, 2 or 3");
+  if (mode < 0 || mode > 2) return set_error(UMT_ERR_ARG, "sweep mode must be 0, 1 or 2");
   if (c.sweepMode != mode) invalidate_graphs(c);
   c.sweepMode = mode;
   return 0;
@@ -881,6 +956,7 @@ int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *t) {
 int umt103_tally_precision(const double *siga, double speed_light, int precision, UmtEnergyTally *t) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (c.rz) return set_error(UMT_ERR_STATE, "umt103_tally: the context holds an RZ problem");
   if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision must be UMT_FP64 or UMT_FP32");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");

@@ -31,25 +31,21 @@ constexpr int kNaChunk = kNaThreads * kNaPerThread;     // elements per block
 
 // File-scope scratch.  Host code must not pass `g_noalloc_scratch` itself to a
 // kernel (on the host that symbol is only a stand-in, not a device address);
-// the device address is obtained once per device with cudaGetSymbolAddress.
+// the device address is looked up with cudaGetSymbolAddress on every call, for
+// the device current at that call.  The lookup allocates nothing; repeating it
+// means a primary context that another library reset and recreated (which
+// reloads the module at a new address) is never served a stale pointer.
 static __device__ __align__(256) double g_noalloc_scratch[4 * UMT_NOALLOC_MAX_BLOCKS + 8];
 
-static double *g_scratch_addr[64];
 static std::mutex g_scratch_mutex;
 
 static int scratch_for_current_device(double **out) {
-  int dev = 0;
-  UMT_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return set_error(UMT_ERR_ARG, "device index %d unsupported", dev);
   std::lock_guard<std::mutex> lk(g_scratch_mutex);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return set_error(UMT_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-    g_scratch_addr[dev] = static_cast<double *>(p);
-  }
-  *out = g_scratch_addr[dev];
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return set_error(UMT_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+  *out = static_cast<double *>(p);
   return 0;
 }
 
@@ -128,6 +124,7 @@ extern "C" int umt103_tally_noalloc(const double *siga_dev, double speed_light, 
                                     UmtEnergyTally *tally) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (c.rz) return set_error(UMT_ERR_STATE, "umt103_tally_noalloc: the context holds an RZ problem");
   if (!tally || !(speed_light > 0.0)) return set_error(UMT_ERR_ARG, "bad tally arguments");
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");

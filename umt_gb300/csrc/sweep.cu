@@ -415,7 +415,13 @@ int record_mid(Ctx &c) {
   return 0;
 }
 
+// A process-wide counter: every invalidation gives the context a fresh
+// generation, so graphs built from its earlier captures (the batch graphs of
+// umt103_batch_sweep) are recognised as stale.
+static unsigned long long g_graph_gen = 0;
+
 void invalidate_graphs(Ctx &c) {
+  c.graphGen = ++g_graph_gen;
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j)
       if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }

@@ -272,227 +272,6 @@ __device__ __forceinline__ void sweep_zone(const Sweep32P &p, const uint2 w, con
   }
 }
 
-// ---------------------------------------------------------------------------
-// Compact-list kernel (groups_per_lane = 2 or 4).  After the zone's corner
-// records are staged, the team classifies its 24 corner-face slots with warp
-// ballots into three bit masks -- incoming FP faces, EZ faces with
-// Omega.A_ez > 0, and those among them whose opposite FP face is incoming --
-// and then walks only the set bits.  Lanes of different zones in one warp
-// diverge only in trip counts, not in per-slot predicates.  All global reads
-// of the zone (previous flux, source, every upwind flux) are issued together
-// as cp.async copies into shared memory.  Arithmetic on group pairs uses
-// Blackwell's paired FP32 instructions (FFMA2/FMUL2/FADD2).
-// ---------------------------------------------------------------------------
-template <int GT, int GPL>
-__global__ void __launch_bounds__(SW32_NT) k_sweep32v4(Sweep32P p, int stage) {
-  static_assert(GPL == 2 || GPL == 4, "paired kernel");
-  constexpr int TEAMS = SW32_NT / GT, NP = GPL / 2, NIT = (24 + GT - 1) / GT;
-  extern __shared__ float4 smem4[];
-  __shared__ float4 sRec[TEAMS][UMT_MAXCORNER][2];
-  __shared__ int4 sConn[TEAMS][UMT_MAXCORNER];
-  const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
-  const int k = blockIdx.x * TEAMS + team;
-  if (k >= p.stageCount[stage]) return;
-  const unsigned tm = team_mask(GT, tid);
-  const int tbase = (tid & 31) / GT * GT;
-  const int G = GT * GPL;
-  float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.stride;   // [8][G] psi_old -> Q
-  float *sS = sQ + 8 * G;                                                    // [8][G] source -> running source
-  float *sP = sS + 8 * G;                                                    // [24][G] upwind fluxes
-  const uint2 w = p.items2[p.stageOffset[stage] + k];
-  const bool bad = (w.x >> 31) != 0;
-  const uint32_t it = w.x & 0x7fffffffu;
-  const int a = (int)(it / (uint32_t)p.nz);
-  const int z = (int)(it - (uint32_t)a * p.nz);
-  const int c0 = (int)(w.y & 0x0fffffffu), nC = (int)(w.y >> 28);
-  const int g0 = lane * GPL;
-  const size_t abase = (size_t)a * p.nc;
-  const float *psiOldA = p.psi_old + abase * G + g0;
-  const float *psiNewA = p.psi_new + abase * G + g0;
-  const float *psiBA = p.psiB + (size_t)a * p.nb * G + g0;
-  // previous flux and source of every corner: asynchronous copies
-  for (int c = 0; c < nC; ++c) {
-    cp_async(sQ + c * G + g0, psiOldA + (size_t)(c0 + c) * G, GPL * 4);
-    cp_async(sS + c * G + g0, p.STotal + (size_t)(c0 + c) * G + g0, GPL * 4);
-  }
-  for (int e = lane; e < 3 * nC; e += GT) {
-    if (e < 2 * nC) sRec[team][e >> 1][e & 1] = p.rec[(abase + c0) * 2 + e];
-    else sConn[team][e - 2 * nC] = p.conn[c0 + e - 2 * nC];
-  }
-  float sig[GPL];
-  vload<GPL>(p.Sigt + (size_t)z * G + g0, sig);
-  const uint32_t ord = p.order[it];
-  __syncwarp(tm);
-  // classify the 24 corner-face slots
-  uint32_t inM = 0, ezM = 0, opM = 0;
-#pragma unroll
-  for (int i = 0; i < NIT; ++i) {
-    const int s = i * GT + lane;
-    bool pin = false, pez = false, pop = false;
-    if (s < 24) {
-      const int c = s / 3, cf = s - 3 * (s / 3);
-      if (c < nC) {
-        const float4 r0 = sRec[team][c][0], r1 = sRec[team][c][1];
-        const int ncf = sConn[team][c].w >> 9;
-        const float af = cf == 0 ? r0.x : (cf == 1 ? r0.y : r0.z);
-        const float ae = cf == 0 ? r1.x : (cf == 1 ? r1.y : r1.z);
-        const int ifp = cf == 2 ? 0 : cf + 1;
-        const float ao = ifp == 0 ? r0.x : (ifp == 1 ? r0.y : r0.z);
-        pin = cf < ncf && af < 0.f;
-        pez = cf < ncf && ae > 0.f;
-        pop = pez && ncf == 3 && ao < 0.f;
-      }
-    }
-    const uint32_t bi = (__ballot_sync(tm, pin) >> tbase) & (GT == 32 ? 0xffffffffu : ((1u << GT) - 1u));
-    const uint32_t be = (__ballot_sync(tm, pez) >> tbase) & (GT == 32 ? 0xffffffffu : ((1u << GT) - 1u));
-    const uint32_t bo = (__ballot_sync(tm, pop) >> tbase) & (GT == 32 ? 0xffffffffu : ((1u << GT) - 1u));
-    inM |= bi << (i * GT);
-    ezM |= be << (i * GT);
-    opM |= bo << (i * GT);
-  }
-  // every upwind flux of the zone: asynchronous copies
-  for (uint32_t m = inM; m; m &= m - 1) {
-    const int s = __ffs(m) - 1;
-    const int c = s / 3, cf = s - 3 * c;
-    const int4 cn = sConn[team][c];
-    const int up = cf == 0 ? cn.x : (cf == 1 ? cn.y : cn.z);
-    const float *src_p = up >= 0 ? psiNewA + (size_t)up * G : psiBA + (size_t)(-up - 1) * G;
-    cp_async(sP + s * G + g0, src_p, GPL * 4);
-  }
-  cp_async_wait_all();
-  const float2 tau2 = f2(p.tau);
-  for (int c = 0; c < nC; ++c) {
-    float2 po[NP], st[NP];
-    ld2<NP>(sQ + c * G + g0, po);
-    ld2<NP>(sS + c * G + g0, st);
-    const float2 v2 = f2(sRec[team][c][1].w);
-#pragma unroll
-    for (int j = 0; j < NP; ++j) {
-      po[j] = __ffma2_rn(tau2, po[j], st[j]);     // Q
-      st[j] = __fmul2_rn(v2, po[j]);              // V*Q
-    }
-    st2<NP>(sQ + c * G + g0, po);
-    st2<NP>(sS + c * G + g0, st);
-  }
-  // incoming FP faces: src_c -= Omega.A_fp * psi_up
-  for (uint32_t m = inM; m; m &= m - 1) {
-    const int s = __ffs(m) - 1;
-    const int c = s / 3, cf = s - 3 * c;
-    const float4 r0 = sRec[team][c][0];
-    const float2 naf = f2(-(cf == 0 ? r0.x : (cf == 1 ? r0.y : r0.z)));
-    float2 pu[NP], sc[NP];
-    ld2<NP>(sP + s * G + g0, pu);
-    ld2<NP>(sS + c * G + g0, sc);
-#pragma unroll
-    for (int j = 0; j < NP; ++j) sc[j] = __ffma2_rn(naf, pu[j], sc[j]);
-    st2<NP>(sS + c * G + g0, sc);
-  }
-  // EZ couplings (closure of SweepUCBxyz.F90:219-256, divided through by aez^4)
-  float2 sg2[NP];
-#pragma unroll
-  for (int j = 0; j < NP; ++j) sg2[j] = make_float2(sig[2 * j], sig[2 * j + 1]);
-  for (uint32_t m = ezM; m; m &= m - 1) {
-    const int s = __ffs(m) - 1;
-    const int c = s / 3, cf = s - 3 * c;
-    const float4 r1 = sRec[team][c][1];
-    const int cez = (sConn[team][c].w >> (3 * cf)) & 7;
-    const float ae = cf == 0 ? r1.x : (cf == 1 ? r1.y : r1.z);
-    const float vol = r1.w;
-    float2 Qc[NP], Qz[NP], sc[NP], sz[NP], sez[NP];
-    ld2<NP>(sQ + c * G + g0, Qc);
-    ld2<NP>(sQ + cez * G + g0, Qz);
-    if ((opM >> s) & 1u) {
-      const int ifp = cf == 2 ? 0 : cf + 1;
-      float2 po[NP];
-      ld2<NP>(sP + (3 * c + ifp) * G + g0, po);
-      const float2 vr = f2(vol * __fdividef(1.0f, ae));
-      const float2 vol2 = f2(vol);
-#pragma unroll
-      for (int j = 0; j < NP; ++j) {
-        float2 x = __fmul2_rn(sg2[j], vr);
-        x.x = fminf(x.x, 1.0e8f); x.y = fminf(x.y, 1.0e8f);
-        const float2 N = __ffma2_rn(__ffma2_rn(f2(1.82f), x, f2(4.f)), x, f2(3.f));
-        const float2 Dh = __ffma2_rn(__ffma2_rn(__ffma2_rn(f2(2.f), x, f2(3.f)), x, f2(2.f)), x, f2(1.f));
-        const float2 den = __ffma2_rn(__fadd2_rn(x, x), Dh, N);
-        const float2 A = __ffma2_rn(sg2[j], po[j], make_float2(-Qc[j].x, -Qc[j].y));
-        const float2 B = __fadd2_rn(Qc[j], make_float2(-Qz[j].x, -Qz[j].y));
-        const float2 num = __ffma2_rn(N, A, __fmul2_rn(Dh, B));
-        sez[j] = __fmul2_rn(vol2, make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y)));
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < NP; ++j) {
-        const float2 h = make_float2(0.5f * ae / sg2[j].x, 0.5f * ae / sg2[j].y);
-        sez[j] = __fmul2_rn(h, __fadd2_rn(Qc[j], make_float2(-Qz[j].x, -Qz[j].y)));
-      }
-    }
-    ld2<NP>(sS + c * G + g0, sc);
-#pragma unroll
-    for (int j = 0; j < NP; ++j) sc[j] = __fadd2_rn(sc[j], sez[j]);
-    st2<NP>(sS + c * G + g0, sc);
-    ld2<NP>(sS + cez * G + g0, sz);
-#pragma unroll
-    for (int j = 0; j < NP; ++j) sz[j] = __fadd2_rn(sz[j], make_float2(-sez[j].x, -sez[j].y));
-    st2<NP>(sS + cez * G + g0, sz);
-  }
-  // corner solve in the schedule's order, EZ exits, boundary exits
-  float *out = p.psi_new + abase * G + g0;
-  float *outB = p.psiB + (size_t)a * p.nb * G + g0;
-  if (bad) {
-    // direct solve: downstream terms from the previous iterate (SweepUCBxyz.F90:283-291)
-    for (int c = 0; c < nC; ++c) {
-      const float4 r1 = sRec[team][c][1];
-      const int4 cn = sConn[team][c];
-      const int ncf = cn.w >> 9;
-      float2 old[NP];
-      ld2<NP>(out + (size_t)(c0 + c) * G, old);
-      const float aez[3] = {r1.x, r1.y, r1.z};
-      for (int cf = 0; cf < 3; ++cf)
-        if (cf < ncf && aez[cf] > 0.f) {
-          const int cez = (cn.w >> (3 * cf)) & 7;
-          float2 t[NP];
-          ld2<NP>(sS + cez * G + g0, t);
-#pragma unroll
-          for (int j = 0; j < NP; ++j) t[j] = __ffma2_rn(f2(aez[cf]), old[j], t[j]);
-          st2<NP>(sS + cez * G + g0, t);
-        }
-    }
-  }
-  for (int i = 0; i < nC; ++i) {
-    const int c = bad ? i : (int)((ord >> (4 * i)) & 15u);
-    const float4 r0 = sRec[team][c][0];
-    const float4 r1 = sRec[team][c][1];
-    const int4 cn = sConn[team][c];
-    const int ncf = cn.w >> 9;
-    float2 sc[NP], v[NP];
-    ld2<NP>(sS + c * G + g0, sc);
-#pragma unroll
-    for (int j = 0; j < NP; ++j) {
-      const float2 dn = __ffma2_rn(sg2[j], f2(r1.w), f2(r0.w));
-      v[j] = make_float2(__fdividef(sc[j].x, dn.x), __fdividef(sc[j].y, dn.y));
-    }
-    st2<NP>(out + (size_t)(c0 + c) * G, v);
-    if (!bad) {
-      const float aez[3] = {r1.x, r1.y, r1.z};
-#pragma unroll
-      for (int cf = 0; cf < 3; ++cf)
-        if (cf < ncf && aez[cf] > 0.f) {
-          const int cez = (cn.w >> (3 * cf)) & 7;
-          float2 t[NP];
-          ld2<NP>(sS + cez * G + g0, t);
-#pragma unroll
-          for (int j = 0; j < NP; ++j) t[j] = __ffma2_rn(f2(aez[cf]), v[j], t[j]);
-          st2<NP>(sS + cez * G + g0, t);
-        }
-    }
-    const float afp[3] = {r0.x, r0.y, r0.z};
-    const int cfp[3] = {cn.x, cn.y, cn.z};
-#pragma unroll
-    for (int cf = 0; cf < 3; ++cf)
-      if (cf < ncf && cfp[cf] < 0 && afp[cf] > 0.f) st2<NP>(outB + (size_t)(-cfp[cf] - 1) * G, v);
-  }
-}
-
 // Level-synchronous form: one launch per dependency stage; the stage's
 // (direction, zone) pairs are independent.
 template <int GT, int GPL>
@@ -646,10 +425,6 @@ int prepare_sweep32(Ctx &c) {
   UMT_ATTR32(4, 1) UMT_ATTR32(4, 2) UMT_ATTR32(4, 4) UMT_ATTR32(8, 1) UMT_ATTR32(8, 2) UMT_ATTR32(8, 4)
   UMT_ATTR32(16, 1) UMT_ATTR32(16, 2) UMT_ATTR32(16, 4) UMT_ATTR32(32, 1) UMT_ATTR32(32, 2) UMT_ATTR32(32, 4)
 #undef UMT_ATTR32
-#define UMT_ATTR4(gt, gpl) TRY_ATTR(allow_dynamic_smem((const void *)k_sweep32v4<gt, gpl>));
-  UMT_ATTR4(1, 2) UMT_ATTR4(1, 4) UMT_ATTR4(2, 2) UMT_ATTR4(2, 4) UMT_ATTR4(4, 2) UMT_ATTR4(4, 4)
-  UMT_ATTR4(8, 2) UMT_ATTR4(8, 4) UMT_ATTR4(16, 2) UMT_ATTR4(16, 4) UMT_ATTR4(32, 2) UMT_ATTR4(32, 4)
-#undef UMT_ATTR4
   const size_t n = (size_t)c.A * c.nc;
   k_corner_rec<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
       c.A, c.nc, c.nCFaces, c.afp64, c.aez64, c.Volume, (float4 *)c.rec32);
@@ -698,30 +473,12 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   int dev = 0, nsm = 0;
   UMT_CUDA(cudaGetDevice(&dev));
   UMT_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int stride4 = 40 * c.G + ((((c.G - (40 * c.G) % 32) % 32) + 32) % 32);
-  const size_t smem4 = (size_t)TEAMS * stride4 * sizeof(float);
   c.exitsThrough = false;
   if (c.sweepMode == 0) {
     const int rc = enqueue_sweep32p(c, cur, GT, GPL);
     if (rc == 0) c.exitsThrough = true;            // the program kernel writes *psibOut's rows
     if (rc <= 0) return rc;                        // 1: no program kernel for this tile
   }
-#define UMT_LAUNCH4(gt, gpl)                                                                       \
-  if (GT == gt && GPL == gpl && c.sweepMode == 3) {                                                \
-    Sweep32P p4 = p;                                                                               \
-    p4.stride = stride4;                                                                           \
-    for (int s = 0; s < c.sch.nStages; ++s) {                                                      \
-      const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;                                    \
-      k_sweep32v4<gt, gpl><<<blocks, 128, smem4, c.stream>>>(p4, s);                               \
-    }                                                                                              \
-    UMT_CUDA(cudaGetLastError());                                                                  \
-    return 0;                                                                                      \
-  }
-  if (c.sweepMode == 3) {
-    UMT_LAUNCH4(1, 2) UMT_LAUNCH4(1, 4) UMT_LAUNCH4(2, 2) UMT_LAUNCH4(2, 4) UMT_LAUNCH4(4, 2) UMT_LAUNCH4(4, 4)
-    UMT_LAUNCH4(8, 2) UMT_LAUNCH4(8, 4) UMT_LAUNCH4(16, 2) UMT_LAUNCH4(16, 4) UMT_LAUNCH4(32, 2) UMT_LAUNCH4(32, 4)
-  }
-#undef UMT_LAUNCH4
 #define UMT_LAUNCH32(gt, gpl)                                                                      \
   if (GT == gt && GPL == gpl) {                                                                    \
     if (c.sweepMode == 1) {                                                                        \

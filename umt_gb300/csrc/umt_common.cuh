@@ -78,6 +78,7 @@ struct Ctx {
   int *dep = nullptr;                           // [A*nz] persistent-mode dependency counters
   int *ticket = nullptr;                        // persistent-mode work ticket
   int holdItem = -1;                            // umt103_hold_item: item given an unsatisfiable dependency
+  unsigned long long graphGen = 0;              // changes whenever this context's captured sweeps go stale
   Schedule sch;
   // materials and sources
   double *Sigt = nullptr, *SigS = nullptr;      // [nz][G]

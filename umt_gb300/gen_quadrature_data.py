@@ -7,7 +7,7 @@ for the 2-D RZ product set).  Directions must be
 identical to the reference's for parity, so the tables are extracted
 verbatim as data by this script (run on a machine that has the source tree):
 
-    python -m umt_gb300.gen_quadrature_data /root/reference
+    python -m umt_gb300.gen_quadrature_data PATH_TO_UMT_SOURCE_TREE
 """
 import re
 import sys
@@ -50,4 +50,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: python -m umt_gb300.gen_quadrature_data PATH_TO_UMT_SOURCE_TREE")
+    main(sys.argv[1])

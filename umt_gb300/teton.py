@@ -4,7 +4,7 @@ Teton's host side is Fortran; no Fortran compiler exists on the machines this
 project builds on, so the routines above the C-ABI are mirrored here with the
 reference's names and argument meaning, calling the CUDA library through
 umt_gb300.capi.  A Fortran caller binds the same C entry points directly
-(INTEGRATION.md).
+through an ISO_C_BINDING interface block.
 
     radtr            aux/radtr.F90:12-71           one radiation cycle
     initializeSets   control/initializeSets.F90:12 tau, Sigt, PsiB, PhiTotal, EnergyRadBOC
