@@ -160,6 +160,14 @@ typedef struct UmtSIParams {
   const double *q_ext;     /* [nzones*G] isotropic external source, or NULL */
   int save_psi;            /* final savePsi sweep                           */
   int warm_start;          /* 1: start from the current PhiTotal, 0: from zero */
+  int learn_every;         /* 0: off; else apply the learned correction after
+                              every learn_every (>= 2) plain iterations; needs
+                              umt103_mlp_init for this group count           */
+  int learn_start;         /* first iteration that may be corrected (>= 2)  */
+  const double *phi_ref;   /* [ncornr*G] or NULL: when given, stop when the
+                              relative L2 distance of PhiTotal to it is below
+                              rel_tol (time-to-converge measurements against a
+                              known converged answer) instead of the change */
 } UmtSIParams;
 
 typedef struct UmtSIResult {
@@ -168,6 +176,8 @@ typedef struct UmtSIResult {
   double rel_change;       /* last relative change of phi                   */
   double seconds;          /* device time                                   */
   int grey_sweeps;         /* GTA grey S2 sweeps performed                  */
+  int learned_kept;        /* learned corrections kept (residual dropped)   */
+  int learned_rejected;    /* learned corrections undone                    */
 } UmtSIResult;
 
 int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);
@@ -227,6 +237,46 @@ int umt103_tally_precision(const double *siga, double speed_light, int precision
 #define UMT_NOALLOC_MAX_BLOCKS 32768
 int umt103_tally_noalloc(const double *siga_dev, double speed_light, int precision,
                          UmtEnergyTally *tally);
+
+/* ---------------------------------------------------------------------------
+ * Learned acceleration of source iteration.  No counterpart in the reference
+ * (Teton accelerates only with grey transport, rt/GTASolver.F90).
+ *
+ * One network per process: per zone, F = 4G+4 features (optical size
+ * ln(sigma_t h), -ln(1-c), the ratio of the last two zone changes of phi, the
+ * signed relative change, and zone size, corner count, corner-volume spread)
+ * -> 3 hidden layers of 128 (ReLU) -> G outputs o; the corrected flux of each
+ * corner is phi + exp(clamp(o, -12, 8)) * (phi - phi_prev).  Weights are
+ * BF16 on the tensor cores with FP32 accumulation (FP32 master copy).  In
+ * umt103_source_iterate (UmtSIParams.learn_every) a correction is kept only
+ * if the next sweep's change of phi is smaller than the change before the
+ * correction; otherwise the iterate is restored.
+ * ------------------------------------------------------------------------- */
+int umt103_mlp_init(int ngr, unsigned seed);          /* random weights; 1 <= ngr <= 60 */
+void umt103_mlp_finalize(void);
+int umt103_mlp_info(int *features, int *hidden, long long *nparams);
+/* FP32 master parameters, in order W1[128][F], b1[128], W2[128][128], b2,
+ * W3[128][128], b3, W4[G][128], b4[G] (row-major, out x in). */
+int umt103_mlp_get_params(float *params);
+int umt103_mlp_set_params(const float *params);
+/* Outputs o [rows][G] of host features X [rows][F] (rounded to BF16). */
+int umt103_mlp_forward(const float *X, int rows, float *Y);
+/* Gradient of sum(dY * o) with respect to every parameter (rows a multiple
+ * of 128), from the same kernels the training uses. */
+int umt103_mlp_gradient(const float *X, const float *dY, int rows, float *grad);
+/* Training set: umt103_mlp_collect appends the current context's zone
+ * features after an (unconverged) umt103_source_iterate of two or more
+ * iterations; umt103_mlp_set_targets(PhiStar) gives the converged PhiTotal
+ * [ncornr][G] of that problem, which sets the targets of every snapshot
+ * collected from it since the last call. */
+int umt103_mlp_collect(int *rows_added);
+int umt103_mlp_set_targets(const double *PhiStar);
+int umt103_mlp_rows(long long *rows);
+int umt103_mlp_clear(void);
+/* Adam on random batches (batch a multiple of 128); loss[0..1] = fraction of
+ * the targets' squared error left after the correction over the first and
+ * last tenth of the steps. */
+int umt103_mlp_train(int steps, int batch, float lr, float *loss);
 
 /* Schedule statistics for one direction. */
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);

@@ -29,6 +29,7 @@ UNITS = {
     "rz.cu": ["-Xcompiler", "-ffp-contract=off"],   # host-side RZ geometry, same rounding as the Fortran
     "noalloc.cu": [],
     "psib.cu": [],
+    "learn.cu": [],
 }
 
 

@@ -53,12 +53,14 @@ class UmtQuadRZ(C.Structure):
 
 class UmtSIParams(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_iters", C.c_int), ("rel_tol", C.c_double),
-                ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int), ("warm_start", C.c_int)]
+                ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int), ("warm_start", C.c_int),
+                ("learn_every", C.c_int), ("learn_start", C.c_int), ("phi_ref", _dp)]
 
 
 class UmtSIResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("sweeps", C.c_int), ("rel_change", C.c_double),
-                ("seconds", C.c_double), ("grey_sweeps", C.c_int)]
+                ("seconds", C.c_double), ("grey_sweeps", C.c_int), ("learned_kept", C.c_int),
+                ("learned_rejected", C.c_int)]
 
 
 class UmtEnergyTally(C.Structure):
@@ -95,8 +97,17 @@ def load():
                   "umt103_set_gta", "umt103_tally_noalloc", "umt103_context_create",
                   "umt103_init_rz", "umt103_sweep_rz", "umt103_get_geometry_rz",
                   "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
-                  "umt103_batch_sweep", "umt103_psib_rows", "umt103_hold_item"):
+                  "umt103_batch_sweep", "umt103_psib_rows", "umt103_hold_item",
+                  "umt103_mlp_init", "umt103_mlp_info", "umt103_mlp_get_params", "umt103_mlp_set_params",
+                  "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect", "umt103_mlp_set_targets",
+                  "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train"):
             getattr(_lib, n).restype = C.c_int
+        _lib.umt103_mlp_finalize.restype = None
+        _fp = C.POINTER(C.c_float)
+        _lib.umt103_mlp_init.argtypes = [C.c_int, C.c_uint]
+        _lib.umt103_mlp_forward.argtypes = [_fp, C.c_int, _fp]
+        _lib.umt103_mlp_gradient.argtypes = [_fp, _fp, C.c_int, _fp]
+        _lib.umt103_mlp_train.argtypes = [C.c_int, C.c_int, C.c_float, _fp]
         _lib.umt103_set_materials.argtypes = [_dp, _dp, C.c_double]
         _lib.umt103_tally.argtypes = [_dp, C.c_double, C.POINTER(UmtEnergyTally)]
         _lib.umt103_tally_precision.argtypes = [_dp, C.c_double, C.c_int, C.POINTER(UmtEnergyTally)]
@@ -113,7 +124,10 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_set_sweep_mode", "umt103_set_gta", "umt103_tally_noalloc",
             "umt103_context_create", "umt103_context_select", "umt103_context_current",
             "umt103_context_destroy", "umt103_batch_sweep", "umt103_init_rz", "umt103_sweep_rz",
-            "umt103_get_geometry_rz", "umt103_psib_rows", "umt103_hold_item"]
+            "umt103_get_geometry_rz", "umt103_psib_rows", "umt103_hold_item",
+            "umt103_mlp_init", "umt103_mlp_finalize", "umt103_mlp_info", "umt103_mlp_get_params",
+            "umt103_mlp_set_params", "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect",
+            "umt103_mlp_set_targets", "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train"]
 
 
 def check(rc):
@@ -233,16 +247,78 @@ class Library:
         return ex.value, tot.value
 
     def source_iterate(self, precision=UMT_FP64, max_iters=50, rel_tol=1e-8, q_ext=None, save_psi=True,
-                       use_gta=False, allow_notconv=False, warm_start=False):
+                       use_gta=False, allow_notconv=False, warm_start=False, learn_every=0, learn_start=2,
+                       phi_ref=None):
         q = _c(q_ext, np.float64)
+        ref = _c(phi_ref, np.float64)
         prm = UmtSIParams(int(precision), int(max_iters), float(rel_tol), int(bool(use_gta)), _d(q),
-                          int(bool(save_psi)), int(bool(warm_start)))
+                          int(bool(save_psi)), int(bool(warm_start)), int(learn_every), int(learn_start), _d(ref))
         res = UmtSIResult()
         rc = self.lib.umt103_source_iterate(C.byref(prm), C.byref(res))
         if rc != 0 and not (allow_notconv and rc == -8):
             check(rc)
         return dict(iterations=res.iterations, sweeps=res.sweeps, rel_change=res.rel_change,
-                    seconds=res.seconds, converged=(rc == 0), grey_sweeps=res.grey_sweeps)
+                    seconds=res.seconds, converged=(rc == 0), grey_sweeps=res.grey_sweeps,
+                    learned_kept=res.learned_kept, learned_rejected=res.learned_rejected)
+
+    # ---- learned acceleration (umt103_mlp_*) ----
+    def mlp_init(self, ngr, seed=0):
+        check(self.lib.umt103_mlp_init(int(ngr), int(seed)))
+
+    def mlp_finalize(self):
+        self.lib.umt103_mlp_finalize()
+
+    def mlp_info(self):
+        f, h, n = C.c_int(0), C.c_int(0), C.c_longlong(0)
+        check(self.lib.umt103_mlp_info(C.byref(f), C.byref(h), C.byref(n)))
+        return f.value, h.value, n.value
+
+    def mlp_get_params(self):
+        p = np.zeros(self.mlp_info()[2], np.float32)
+        check(self.lib.umt103_mlp_get_params(p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    def mlp_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(self.lib.umt103_mlp_set_params(p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def mlp_forward(self, X, G):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], G), np.float32)
+        fp = C.POINTER(C.c_float)
+        check(self.lib.umt103_mlp_forward(X.ctypes.data_as(fp), X.shape[0], Y.ctypes.data_as(fp)))
+        return Y
+
+    def mlp_gradient(self, X, dY):
+        X = np.ascontiguousarray(X, dtype=np.float32); dY = np.ascontiguousarray(dY, dtype=np.float32)
+        g = np.zeros(self.mlp_info()[2], np.float32)
+        fp = C.POINTER(C.c_float)
+        check(self.lib.umt103_mlp_gradient(X.ctypes.data_as(fp), dY.ctypes.data_as(fp), X.shape[0],
+                                           g.ctypes.data_as(fp)))
+        return g
+
+    def mlp_collect(self):
+        n = C.c_int(0)
+        check(self.lib.umt103_mlp_collect(C.byref(n)))
+        return n.value
+
+    def mlp_set_targets(self, PhiStar):
+        PhiStar = _c(PhiStar, np.float64)
+        check(self.lib.umt103_mlp_set_targets(_d(PhiStar)))
+
+    def mlp_rows(self):
+        n = C.c_longlong(0)
+        check(self.lib.umt103_mlp_rows(C.byref(n)))
+        return n.value
+
+    def mlp_clear(self):
+        check(self.lib.umt103_mlp_clear())
+
+    def mlp_train(self, steps, batch=4096, lr=1e-3):
+        loss = np.zeros(2, np.float32)
+        check(self.lib.umt103_mlp_train(int(steps), int(batch), C.c_float(lr),
+                                        loss.ctypes.data_as(C.POINTER(C.c_float))))
+        return float(loss[0]), float(loss[1])
 
     def tally(self, siga=None, speed_light=299.792458, precision=None):
         siga = _c(siga, np.float64)

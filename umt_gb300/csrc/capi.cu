@@ -68,7 +68,8 @@ static void free_ctx(Ctx &c) {
   dfree(s.needInit); dfree(c.dep); dfree(c.ticket);
   dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
-  dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red);
+  dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red); dfree(c.siDelta); dfree(c.siDeltaPrev); dfree(c.siKeep);
+  dfree(c.siState); dfree(c.siRef);
   dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
@@ -884,6 +885,98 @@ static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps) {
   return gta_correct(c, x);
 }
 
+// ---------------------------------------------------------------------------
+// Source iteration as one CUDA graph launch: a conditional WHILE node whose
+// body is build-source -> sweep -> change norm (-> distance to phi_ref) ->
+// k_si_decide, which counts the iteration, forms the convergence criterion
+// on the device and sets the loop condition.  The host waits once, at the
+// end.  Used for plain iterations (no GTA, no learned step: those decide on
+// the host); a context where the graph cannot be built keeps the host loop.
+// ---------------------------------------------------------------------------
+struct SIState {
+  int it, maxit, conv, useRef;
+  double tol, rel, dist;
+};
+
+__global__ void k_si_reset(SIState *s, int maxit, double tol, int useRef) {
+  s->it = 0; s->maxit = maxit; s->conv = 0; s->useRef = useRef;
+  s->tol = tol; s->rel = 1.0; s->dist = -1.0;
+}
+
+__global__ void k_si_decide(cudaGraphConditionalHandle h, SIState *s, const double *red) {
+  const double rel = red[1] > 0.0 ? sqrt(red[0] / red[1]) : 0.0;
+  double crit = rel;
+  if (s->useRef) {
+    crit = red[3] > 0.0 ? sqrt(red[2] / red[3]) : 0.0;
+    s->dist = crit;
+  }
+  s->rel = rel;
+  s->it += 1;
+  s->conv = crit < s->tol ? 1 : 0;
+  cudaGraphSetConditional(h, (!s->conv && s->it < s->maxit) ? 1u : 0u);
+}
+
+// Builds (once per precision, buffer parity and criterion) and returns the
+// graph; 1 when this context cannot use one.
+static int si_graph(Ctx &c, int prec, const double *q, bool useRef, cudaGraphExec_t *out) {
+  const int cur = prec == UMT_FP64 ? c.cur64 : c.cur32;
+  cudaGraphExec_t &ex = c.siGraph[prec][cur][useRef ? 1 : 0];
+  if (ex) { *out = ex; return 0; }
+  if (c.siGraphState < 0) return 1;
+  if (prec == UMT_FP32) {                          // one-time FP32 preparation, outside any capture
+    bool prog = false;
+    TRY(fp32_program_path(c, &prog));
+  }
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  int rc = 0;
+  if (e == cudaSuccess) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const bool graphs = c.useGraphs;
+      c.useGraphs = false;                         // enqueue the sweep's kernels into the body
+      c.inSIGraph = true;
+      rc = launch_build_source(c, q);
+      if (!rc) rc = launch_sweep_once(c, prec, true);
+      if (!rc) rc = launch_change_norm(c, c.PhiPrev, c.red, c.siDelta, c.siDeltaPrev);
+      if (!rc && useRef) rc = launch_distance(c, c.siRef, c.red + 2);
+      if (!rc) {
+        k_si_decide<<<1, 1, 0, c.stream>>>(h, (SIState *)c.siState, c.red);
+        if (cudaGetLastError() != cudaSuccess) rc = set_error(UMT_ERR_CUDA, "si graph: decide launch");
+      }
+      c.inSIGraph = false;
+      c.useGraphs = graphs;
+      cudaGraph_t got = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(c.stream, &got);
+      if (e == cudaSuccess) e = e2;
+    }
+  }
+  if (!rc && e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (rc) { cudaGetLastError(); return rc; }
+  if (e != cudaSuccess || !exec) {
+    // conditional bodies refuse some node kinds; this context keeps the host loop
+    cudaGetLastError();
+    c.siGraphState = -1;
+    return 1;
+  }
+  c.siGraphState = 1;
+  ex = exec;
+  *out = exec;
+  return 0;
+}
+
 int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
@@ -904,6 +997,26 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   const size_t ncG = (size_t)c.nc * c.G, nzG = (size_t)c.nz * c.G;
   if (!c.PhiPrev) TRY(dalloc(&c.PhiPrev, ncG));
   if (!c.red) TRY(dalloc(&c.red, 8));
+  const int learnEvery = prm->learn_every;
+  if (learnEvery < 0) return set_error(UMT_ERR_ARG, "learn_every must be >= 0");
+  if (learnEvery > 0 && !mlp_ready_for(c.G))
+    return set_error(UMT_ERR_STATE, "learned correction requested but no model for G=%d (umt103_mlp_init)", c.G);
+  // the last two changes of PhiTotal (features of the learned step, and the
+  // training snapshots of umt103_mlp_collect)
+  if (!c.siDelta) TRY(dalloc(&c.siDelta, ncG));
+  if (!c.siDeltaPrev) TRY(dalloc(&c.siDeltaPrev, ncG));
+  if (learnEvery > 0 && !c.siKeep) TRY(dalloc(&c.siKeep, ncG));
+  UMT_CUDA(cudaMemsetAsync(c.siDelta, 0, ncG * 8, c.stream));
+  UMT_CUDA(cudaMemsetAsync(c.siDeltaPrev, 0, ncG * 8, c.stream));
+  double *ref = nullptr;                          // device copy of phi_ref (this call only)
+  if (prm->phi_ref) {
+    TRY(dalloc(&ref, ncG));
+    if (cudaMemcpy(ref, prm->phi_ref, ncG * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(ref);
+      return set_error(UMT_ERR_CUDA, "phi_ref upload failed");
+    }
+  }
+  struct RefGuard { double *p; ~RefGuard() { if (p) cudaFree(p); } } refGuard{ref};
   const double *q = nullptr;
   if (prm->q_ext) {
     if (!c.qExt) TRY(dalloc(&c.qExt, nzG));
@@ -916,22 +1029,81 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   cudaEvent_t t0, t1;
   UMT_CUDA(cudaEventCreate(&t0)); UMT_CUDA(cudaEventCreate(&t1));
   UMT_CUDA(cudaEventRecord(t0, c.stream));
-  int it = 0, sweeps = 0;
-  double rel = 1.0;
-  bool conv = false;
-  while (it < maxit) {
+  int it = 0, sweeps = 0, kept = 0, rejected = 0, plain = 0;
+  const int learnStart = std::max(prm->learn_start, 2);
+  double rel = 1.0, rBefore = 0.0;
+  bool conv = false, pending = false;
+  bool viaGraph = false;
+  if (!prm->use_gta && learnEvery == 0 && c.useGraphs && c.siGraphState >= 0) {
+    if (!c.siState) TRY(dalloc((SIState **)&c.siState, 1));
+    if (ref && !c.siRef) TRY(dalloc(&c.siRef, ncG));
+    cudaGraphExec_t ex = nullptr;
+    const int grc = si_graph(c, prec, q, ref != nullptr, &ex);
+    if (grc < 0) return grc;
+    if (grc == 0) {
+      viaGraph = true;
+      if (ref) UMT_CUDA(cudaMemcpyAsync(c.siRef, ref, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+      k_si_reset<<<1, 1, 0, c.stream>>>((SIState *)c.siState, maxit, prm->rel_tol, ref ? 1 : 0);
+      UMT_CUDA(cudaGetLastError());
+      UMT_CUDA(cudaEventRecord(t0, c.stream));   // timing starts at the graph launch
+      UMT_CUDA(cudaGraphLaunch(ex, c.stream));
+      SIState st;
+      UMT_CUDA(cudaMemcpyAsync(&st, c.siState, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+      UMT_CUDA(cudaStreamSynchronize(c.stream));
+      it = st.it; sweeps = st.it; rel = st.rel; conv = st.conv != 0;
+    }
+  }
+  while (!viaGraph && it < maxit) {
     ++it;
     TRY(launch_build_source(c, q));
     TRY(launch_sweep_once(c, prec, true));
     ++sweeps;
     if (prm->use_gta) TRY(gta_solve(c, c.gtaMaxKrylov, c.gtaTol, &greySweeps));
-    TRY(launch_change_norm(c, c.PhiPrev, c.red));
+    TRY(launch_change_norm(c, c.PhiPrev, c.red, c.siDelta, c.siDeltaPrev));
     double h[2];
     UMT_CUDA(cudaMemcpyAsync(h, c.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UMT_CUDA(cudaStreamSynchronize(c.stream));
     rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
-    if (rel < prm->rel_tol) { conv = true; break; }
+    const double rAbs = std::sqrt(h[0]);
+    double dist = -1.0;                           // relative distance to phi_ref
+    if (ref) {
+      TRY(launch_distance(c, ref, c.red + 2));
+      UMT_CUDA(cudaMemcpyAsync(h, c.red + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      UMT_CUDA(cudaStreamSynchronize(c.stream));
+      dist = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    }
+    if (pending) {
+      // The sweep after a learned correction is its check: the correction
+      // stays only if the iteration residual dropped below the one before it.
+      pending = false;
+      if (rAbs < rBefore) {
+        ++kept;
+      } else {
+        ++rejected;
+        UMT_CUDA(cudaMemcpyAsync(c.Phi, c.siKeep, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+        UMT_CUDA(cudaMemcpyAsync(c.PhiPrev, c.siKeep, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+        plain = 0;
+        rel = 1.0;
+        continue;
+      }
+    }
+    if ((ref ? dist : rel) < prm->rel_tol) { conv = true; break; }
+    ++plain;
+    // two plain iterations since the last correction give the change ratio
+    if (learnEvery > 0 && it >= learnStart && plain >= std::max(learnEvery, 2)) {
+      UMT_CUDA(cudaMemcpyAsync(c.siKeep, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+      TRY(mlp_correct(c, c.siDelta, c.siDeltaPrev));
+      UMT_CUDA(cudaMemcpyAsync(c.PhiPrev, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+      rBefore = rAbs;
+      pending = true;
+      plain = 0;
+    }
   }
+  if (pending) {                                  // the last correction was never checked: undo it
+    UMT_CUDA(cudaMemcpyAsync(c.Phi, c.siKeep, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+    ++rejected;
+  }
+  if (learnEvery > 0) TRY(mlp_status());
   if (prm->save_psi) {
     TRY(launch_build_source(c, q));
     TRY(launch_sweep_once(c, prec, true));
@@ -945,6 +1117,8 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   cudaEventDestroy(t0); cudaEventDestroy(t1);
   res->iterations = it; res->sweeps = sweeps; res->rel_change = rel; res->seconds = ms * 1e-3;
   res->grey_sweeps = greySweeps;
+  res->learned_kept = kept;
+  res->learned_rejected = rejected;
   return conv ? 0 : set_error(UMT_ERR_NOTCONV, "not converged after %d iterations (rel change %.3e)", it, rel);
 }
 

@@ -48,14 +48,31 @@ __device__ void block_reduce_add(double (&v)[NV], double *out) {
   }
 }
 
-// sum (phi - prev)^2, sum phi^2; then prev = phi
-__global__ void k_change_norm(size_t n, const double *Phi, double *prev, double *out2) {
+// sum (phi - prev)^2, sum phi^2; then prev = phi.  With delta given, the
+// change is kept too (deltaPrev, if given, receives the change before it).
+__global__ void k_change_norm(size_t n, const double *Phi, double *prev, double *out2, double *delta,
+                              double *deltaPrev) {
   double v[2] = {0.0, 0.0};
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const double d = Phi[i] - prev[i];
     v[0] += d * d;
     v[1] += Phi[i] * Phi[i];
     prev[i] = Phi[i];
+    if (delta) {
+      if (deltaPrev) deltaPrev[i] = delta[i];
+      delta[i] = d;
+    }
+  }
+  block_reduce_add<2>(v, out2);
+}
+
+// sum (phi - ref)^2, sum ref^2
+__global__ void k_distance(size_t n, const double *Phi, const double *ref, double *out2) {
+  double v[2] = {0.0, 0.0};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double d = Phi[i] - ref[i];
+    v[0] += d * d;
+    v[1] += ref[i] * ref[i];
   }
   block_reduce_add<2>(v, out2);
 }
@@ -261,10 +278,17 @@ int launch_build_source(Ctx &c, const double *q) {
   return 0;
 }
 
-int launch_change_norm(Ctx &c, double *prev, double *out2) {
+int launch_change_norm(Ctx &c, double *prev, double *out2, double *delta, double *deltaPrev) {
   const size_t n = (size_t)c.nc * c.G;
   UMT_CUDA(cudaMemsetAsync(out2, 0, 2 * sizeof(double), c.stream));
-  k_change_norm<<<152 * 4, 256, 0, c.stream>>>(n, c.Phi, prev, out2);
+  k_change_norm<<<152 * 4, 256, 0, c.stream>>>(n, c.Phi, prev, out2, delta, deltaPrev);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int launch_distance(Ctx &c, const double *ref, double *out2) {
+  UMT_CUDA(cudaMemsetAsync(out2, 0, 2 * sizeof(double), c.stream));
+  k_distance<<<152 * 4, 256, 0, c.stream>>>((size_t)c.nc * c.G, c.Phi, ref, out2);
   UMT_CUDA(cudaGetLastError());
   return 0;
 }

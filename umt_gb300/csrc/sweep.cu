@@ -366,7 +366,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
       default: k_sweep<T, 32><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
     }
   }
-  TRY_RC(record_mid(c));
+  if (!c.inSIGraph) TRY_RC(record_mid(c));       // no event nodes inside a conditional body
   const size_t ncG = (size_t)c.nc * c.G;
   const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
   if constexpr (sizeof(T) == 4) {
@@ -427,6 +427,10 @@ void invalidate_graphs(Ctx &c) {
       if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
   for (auto &g : c.graphsWT)
     if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+  for (auto &a : c.siGraph)
+    for (auto &b : a)
+      for (auto &g : b)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
 }
 
 // Capture one sweep (source conversion, every dependency stage, tally) for

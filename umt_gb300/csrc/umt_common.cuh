@@ -89,6 +89,17 @@ struct Ctx {
   double *Phi = nullptr;                        // [nc][G]
   double *PhiPrev = nullptr;                    // [nc][G] previous iterate
   double *qExt = nullptr;                       // [nz][G] isotropic source
+  double *siDelta = nullptr;                    // [nc][G] last change of PhiTotal in source iteration
+  double *siDeltaPrev = nullptr;                // [nc][G] the change before it
+  double *siKeep = nullptr;                     // [nc][G] iterate before a learned correction (kept for rollback)
+  double hMean = 0.0;                           // mean zone size, (total volume / nz)^(1/3)
+  // source iteration as one graph: a conditional while node around
+  // build-source, sweep, change norm and a device-side convergence decision
+  void *siState = nullptr;                      // device SIState (capi.cu)
+  double *siRef = nullptr;                      // [nc][G] device copy of UmtSIParams.phi_ref
+  cudaGraphExec_t siGraph[2][2][2] = {};        // [precision][cur][with phi_ref]
+  bool inSIGraph = false;                       // enqueueing into that graph's body (no event records)
+  int siGraphState = 0;                         // 0 untried, 1 works, -1 unavailable (host loop)
   double *red = nullptr;                        // [8] reduction slots
   // angular flux, double buffered: psi[cur] = saved Psi, psi[1-cur] = new
   double *psi64[2] = {nullptr, nullptr};
@@ -160,8 +171,13 @@ int record_mid(Ctx &c);
 int launch_convert_source(Ctx &c);
 // source iteration and edits (si.cu)
 int launch_build_source(Ctx &c, const double *q);
-int launch_change_norm(Ctx &c, double *prev, double *out2);
+int launch_change_norm(Ctx &c, double *prev, double *out2, double *delta = nullptr, double *deltaPrev = nullptr);
+// learned correction (learn.cu)
+bool mlp_ready_for(int G);
+int mlp_correct(Ctx &c, const double *Delta, const double *DeltaPrev);
+int mlp_status();
 int launch_energy(Ctx &c, const double *siga_dev, int precision, double *out4);
+int launch_distance(Ctx &c, const double *ref, double *out2);
 // grey transport acceleration (si.cu)
 int gta_prepare(Ctx &c);
 int gta_apply(Ctx &c, const double *x, double wR);
