@@ -39,8 +39,9 @@ enum {
   UMT_ERR_NOTCONV = -8     /* iteration limit reached before convergence   */
 };
 
-/* precision of the angular-flux sweep */
-enum { UMT_FP64 = 0, UMT_FP32 = 1 };
+/* precision of the angular-flux sweep; UMT_MIXED (source iteration only):
+ * FP64 residual sweeps around FP32 correction solves */
+enum { UMT_FP64 = 0, UMT_FP32 = 1, UMT_MIXED = 2 };
 
 /*
  * Mesh in Teton's corner representation: what teton_setzone
@@ -151,9 +152,20 @@ int umt103_set_source(const double *STotal);
 int umt103_sweep_resident(int savePsi, int precision);
 int umt103_get_phi(double *PhiTotal);
 
-/* Source iteration (rtmainsn / LinearSolver / ConvergenceTest). */
+/* Source iteration (rtmainsn / LinearSolver / ConvergenceTest).
+ *
+ * UMT_MIXED is defect correction: each outer step is one FP64 sweep of the
+ * current iterate X, giving the exact residual R = T(X) - X of the
+ * source-iteration map T; the correction D solving D = K D + R (K: the
+ * scattering sweep with no tau*psi_old term and no boundary inflow) is then
+ * iterated with FP32 sweeps until its relative change is below inner_tol,
+ * and X += D.  The FP32 rounding then limits only the correction, so the
+ * iteration reaches FP64 accuracy where plain FP32 source iteration stalls
+ * at an error of about (FP32 rounding) / (1 - c) in strongly scattering
+ * zones.  The learned step (learn_every) acts on the inner iteration.  No
+ * counterpart in the reference (FP64 throughout). */
 typedef struct UmtSIParams {
-  int precision;           /* UMT_FP64 or UMT_FP32                          */
+  int precision;           /* UMT_FP64, UMT_FP32 or UMT_MIXED               */
   int max_iters;           /* outer iterations (default 50)                 */
   double rel_tol;          /* max relative change of zone phi               */
   int use_gta;             /* 1: grey transport acceleration after each sweep */
@@ -168,6 +180,9 @@ typedef struct UmtSIParams {
                               relative L2 distance of PhiTotal to it is below
                               rel_tol (time-to-converge measurements against a
                               known converged answer) instead of the change */
+  double inner_tol;        /* UMT_MIXED: relative change ending a correction
+                              solve (0: 1e-3)                                */
+  int inner_max;           /* UMT_MIXED: FP32 sweeps per correction (0: 500) */
 } UmtSIParams;
 
 typedef struct UmtSIResult {
@@ -178,6 +193,7 @@ typedef struct UmtSIResult {
   int grey_sweeps;         /* GTA grey S2 sweeps performed                  */
   int learned_kept;        /* learned corrections kept (residual dropped)   */
   int learned_rejected;    /* learned corrections undone                    */
+  int fp64_sweeps;         /* sweeps with the FP64 angular flux             */
 } UmtSIResult;
 
 int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);

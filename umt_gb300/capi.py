@@ -14,7 +14,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libumt103.so")
 
-UMT_FP64, UMT_FP32 = 0, 1
+UMT_FP64, UMT_FP32, UMT_MIXED = 0, 1, 2
 (UMT_OK, UMT_ERR_ARG, UMT_ERR_STATE, UMT_ERR_CUDA, UMT_ERR_CYCLE, UMT_ERR_TIMEOUT, UMT_ERR_BOUNDS,
  UMT_ERR_NOMEM, UMT_ERR_NOTCONV) = (0, -1, -2, -3, -4, -5, -6, -7, -8)
 
@@ -54,13 +54,14 @@ class UmtQuadRZ(C.Structure):
 class UmtSIParams(C.Structure):
     _fields_ = [("precision", C.c_int), ("max_iters", C.c_int), ("rel_tol", C.c_double),
                 ("use_gta", C.c_int), ("q_ext", _dp), ("save_psi", C.c_int), ("warm_start", C.c_int),
-                ("learn_every", C.c_int), ("learn_start", C.c_int), ("phi_ref", _dp)]
+                ("learn_every", C.c_int), ("learn_start", C.c_int), ("phi_ref", _dp),
+                ("inner_tol", C.c_double), ("inner_max", C.c_int)]
 
 
 class UmtSIResult(C.Structure):
     _fields_ = [("iterations", C.c_int), ("sweeps", C.c_int), ("rel_change", C.c_double),
                 ("seconds", C.c_double), ("grey_sweeps", C.c_int), ("learned_kept", C.c_int),
-                ("learned_rejected", C.c_int)]
+                ("learned_rejected", C.c_int), ("fp64_sweeps", C.c_int)]
 
 
 class UmtEnergyTally(C.Structure):
@@ -248,18 +249,20 @@ class Library:
 
     def source_iterate(self, precision=UMT_FP64, max_iters=50, rel_tol=1e-8, q_ext=None, save_psi=True,
                        use_gta=False, allow_notconv=False, warm_start=False, learn_every=0, learn_start=2,
-                       phi_ref=None):
+                       phi_ref=None, inner_tol=0.0, inner_max=0):
         q = _c(q_ext, np.float64)
         ref = _c(phi_ref, np.float64)
         prm = UmtSIParams(int(precision), int(max_iters), float(rel_tol), int(bool(use_gta)), _d(q),
-                          int(bool(save_psi)), int(bool(warm_start)), int(learn_every), int(learn_start), _d(ref))
+                          int(bool(save_psi)), int(bool(warm_start)), int(learn_every), int(learn_start), _d(ref),
+                          float(inner_tol), int(inner_max))
         res = UmtSIResult()
         rc = self.lib.umt103_source_iterate(C.byref(prm), C.byref(res))
         if rc != 0 and not (allow_notconv and rc == -8):
             check(rc)
         return dict(iterations=res.iterations, sweeps=res.sweeps, rel_change=res.rel_change,
                     seconds=res.seconds, converged=(rc == 0), grey_sweeps=res.grey_sweeps,
-                    learned_kept=res.learned_kept, learned_rejected=res.learned_rejected)
+                    learned_kept=res.learned_kept, learned_rejected=res.learned_rejected,
+                    fp64_sweeps=res.fp64_sweeps)
 
     # ---- learned acceleration (umt103_mlp_*) ----
     def mlp_init(self, ngr, seed=0):

@@ -69,7 +69,7 @@ static void free_ctx(Ctx &c) {
   dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red); dfree(c.siDelta); dfree(c.siDeltaPrev); dfree(c.siKeep);
-  dfree(c.siState); dfree(c.siRef);
+  dfree(c.siState); dfree(c.siRef); dfree(c.psiB32h); dfree(c.mixX); dfree(c.mixR); dfree(c.mixD);
   dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
@@ -907,7 +907,7 @@ __global__ void k_si_decide(cudaGraphConditionalHandle h, SIState *s, const doub
   const double rel = red[1] > 0.0 ? sqrt(red[0] / red[1]) : 0.0;
   double crit = rel;
   if (s->useRef) {
-    crit = red[3] > 0.0 ? sqrt(red[2] / red[3]) : 0.0;
+    crit = red[9] > 0.0 ? sqrt(red[8] / red[9]) : 0.0;
     s->dist = crit;
   }
   s->rel = rel;
@@ -950,7 +950,7 @@ static int si_graph(Ctx &c, int prec, const double *q, bool useRef, cudaGraphExe
       rc = launch_build_source(c, q);
       if (!rc) rc = launch_sweep_once(c, prec, true);
       if (!rc) rc = launch_change_norm(c, c.PhiPrev, c.red, c.siDelta, c.siDeltaPrev);
-      if (!rc && useRef) rc = launch_distance(c, c.siRef, c.red + 2);
+      if (!rc && useRef) rc = launch_distance(c, c.siRef, c.red + 8);
       if (!rc) {
         k_si_decide<<<1, 1, 0, c.stream>>>(h, (SIState *)c.siState, c.red);
         if (cudaGetLastError() != cudaSuccess) rc = set_error(UMT_ERR_CUDA, "si graph: decide launch");
@@ -977,13 +977,121 @@ static int si_graph(Ctx &c, int prec, const double *q, bool useRef, cudaGraphExe
   return 0;
 }
 
+// Mixed-precision source iteration (UMT_MIXED): FP64 residual sweeps, FP32
+// correction solves, the learned step inside the correction solves.
+struct MixedStats { int outer = 0, fp32 = 0, fp64 = 0, kept = 0, rejected = 0; double rel = 1.0; bool conv = false; };
+
+static int mixed_iterate(Ctx &c, const UmtSIParams *prm, const double *q, const double *ref, MixedStats &st) {
+  const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
+  if (!c.psi64[0] || !c.psi32[0]) return set_error(UMT_ERR_STATE, "UMT_MIXED needs both the FP64 and the FP32 flux");
+  if (!c.mixX) TRY(dalloc(&c.mixX, ncG));
+  if (!c.mixR) TRY(dalloc(&c.mixR, ncG));
+  if (!c.mixD) TRY(dalloc(&c.mixD, ncG));
+  if (!c.psiB32h) {
+    TRY(dalloc(&c.psiB32h, psiBN));
+    UMT_CUDA(cudaMemset(c.psiB32h, 0, psiBN * sizeof(float)));
+  }
+  const int maxit = prm->max_iters > 0 ? prm->max_iters : 50;
+  const double innerTol = prm->inner_tol > 0.0 ? prm->inner_tol : 1e-3;
+  const int innerMax = prm->inner_max > 0 ? prm->inner_max : 500;
+  const int learnEvery = prm->learn_every;
+  const int learnStart = std::max(prm->learn_start, 2);
+  if (prm->warm_start) UMT_CUDA(cudaMemcpyAsync(c.mixX, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+  else UMT_CUDA(cudaMemsetAsync(c.mixX, 0, ncG * 8, c.stream));
+  struct Homog {                                  // the homogeneous FP32 sweeps end with the call
+    Ctx &c;
+    ~Homog() { c.homog32 = false; }
+  } homogGuard{c};
+  double h[3];
+  auto fetch2 = [&](const double *dev) -> int {
+    UMT_CUDA(cudaMemcpyAsync(h, dev, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    UMT_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+  };
+  while (st.outer < maxit) {
+    ++st.outer;
+    // exact residual of the current iterate: one FP64 sweep
+    c.homog32 = false;
+    TRY(launch_build_source_vec(c, c.mixX, q));
+    TRY(launch_sweep_once(c, UMT_FP64, true));
+    ++st.fp64;
+    TRY(launch_residual(c, c.mixX, c.mixR, c.red));
+    TRY(fetch2(c.red));
+    st.rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    double crit = st.rel;
+    if (ref) {                                    // T(X) is the better iterate: judge it
+      TRY(launch_distance(c, ref, c.red + 8));
+      TRY(fetch2(c.red + 8));
+      crit = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
+    }
+    if (crit < prm->rel_tol) {
+      UMT_CUDA(cudaMemcpyAsync(c.mixX, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+      st.conv = true;
+      break;
+    }
+    // correction D = K D + R by FP32 source iteration from D = R
+    c.homog32 = true;
+    UMT_CUDA(cudaMemcpyAsync(c.mixD, c.mixR, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+    UMT_CUDA(cudaMemcpyAsync(c.siDelta, c.mixR, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+    UMT_CUDA(cudaMemsetAsync(c.siDeltaPrev, 0, ncG * 8, c.stream));
+    int plain = 1;
+    bool pending = false;
+    double rBefore = 0.0;
+    for (int j = 1; j < innerMax; ++j) {
+      TRY(launch_build_source_vec(c, c.mixD, nullptr));
+      TRY(launch_sweep_once(c, UMT_FP32, true));
+      ++st.fp32;
+      TRY(launch_inner_update(c, c.mixR, c.mixD, c.siDelta, c.siDeltaPrev, c.red));
+      TRY(fetch2(c.red));
+      const double dAbs = std::sqrt(h[2]);            // amplification-weighted change
+      const double relIn = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
+      if (pending) {
+        pending = false;
+        if (dAbs < rBefore) {
+          ++st.kept;
+        } else {
+          ++st.rejected;
+          UMT_CUDA(cudaMemcpyAsync(c.mixD, c.siKeep, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+          plain = 0;
+          continue;
+        }
+      }
+      if (relIn < innerTol) break;
+      ++plain;
+      if (learnEvery > 0 && j + 1 >= learnStart && plain >= std::max(learnEvery, 2)) {
+        UMT_CUDA(cudaMemcpyAsync(c.siKeep, c.mixD, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+        TRY(mlp_correct(c, c.mixD, c.siDelta, c.siDeltaPrev));
+        rBefore = dAbs;
+        pending = true;
+        plain = 0;
+      }
+    }
+    if (pending) {                                // unchecked: undo
+      UMT_CUDA(cudaMemcpyAsync(c.mixD, c.siKeep, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+      ++st.rejected;
+    }
+    c.homog32 = false;
+    TRY(gta_axpbypcz(c, (int)ncG, 1.0, c.mixD, 1.0, c.mixX, 0.0, nullptr));     // X += D
+    if (ref) {
+      TRY(launch_distance(c, ref, c.red + 8, c.mixX));
+      TRY(fetch2(c.red + 8));
+      if ((h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0) < prm->rel_tol) { st.conv = true; break; }
+    }
+  }
+  UMT_CUDA(cudaMemcpyAsync(c.Phi, c.mixX, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+  UMT_CUDA(cudaMemcpyAsync(c.PhiPrev, c.mixX, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
+  if (learnEvery > 0) TRY(mlp_status());
+  return 0;
+}
+
 int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem: use umt103_sweep_rz");
   if (!prm || !res) return set_error(UMT_ERR_ARG, "null params/result");
   const int prec = prm->precision;
-  if (prec != UMT_FP64 && prec != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
+  if (prec != UMT_FP64 && prec != UMT_FP32 && prec != UMT_MIXED) return set_error(UMT_ERR_ARG, "precision");
+  if (prec == UMT_MIXED && prm->use_gta) return set_error(UMT_ERR_ARG, "UMT_MIXED does not combine with GTA");
   if (prm->use_gta && !c.gta) return set_error(UMT_ERR_STATE, "GTA context not created (init flag 8 set)");
   if (prm->use_gta) {
     if (!c.gtaChi) TRY(dalloc(&c.gtaChi, (size_t)c.nz * c.G));
@@ -996,7 +1104,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   int greySweeps = 0;
   const size_t ncG = (size_t)c.nc * c.G, nzG = (size_t)c.nz * c.G;
   if (!c.PhiPrev) TRY(dalloc(&c.PhiPrev, ncG));
-  if (!c.red) TRY(dalloc(&c.red, 8));
+  if (!c.red) TRY(dalloc(&c.red, 16));
   const int learnEvery = prm->learn_every;
   if (learnEvery < 0) return set_error(UMT_ERR_ARG, "learn_every must be >= 0");
   if (learnEvery > 0 && !mlp_ready_for(c.G))
@@ -1034,7 +1142,15 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   double rel = 1.0, rBefore = 0.0;
   bool conv = false, pending = false;
   bool viaGraph = false;
-  if (!prm->use_gta && learnEvery == 0 && c.useGraphs && c.siGraphState >= 0) {
+  const bool mixed = prec == UMT_MIXED;
+  int fp64Sweeps = 0;
+  if (mixed) {
+    MixedStats ms;
+    TRY(mixed_iterate(c, prm, q, ref, ms));
+    it = ms.outer; sweeps = ms.fp32 + ms.fp64; fp64Sweeps = ms.fp64; rel = ms.rel; conv = ms.conv;
+    kept = ms.kept; rejected = ms.rejected;
+  }
+  if (!mixed && !prm->use_gta && learnEvery == 0 && c.useGraphs && c.siGraphState >= 0) {
     if (!c.siState) TRY(dalloc((SIState **)&c.siState, 1));
     if (ref && !c.siRef) TRY(dalloc(&c.siRef, ncG));
     cudaGraphExec_t ex = nullptr;
@@ -1053,28 +1169,33 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
       it = st.it; sweeps = st.it; rel = st.rel; conv = st.conv != 0;
     }
   }
-  while (!viaGraph && it < maxit) {
+  while (!viaGraph && !mixed && it < maxit) {
     ++it;
     TRY(launch_build_source(c, q));
     TRY(launch_sweep_once(c, prec, true));
     ++sweeps;
     if (prm->use_gta) TRY(gta_solve(c, c.gtaMaxKrylov, c.gtaTol, &greySweeps));
-    TRY(launch_change_norm(c, c.PhiPrev, c.red, c.siDelta, c.siDeltaPrev));
-    double h[2];
-    UMT_CUDA(cudaMemcpyAsync(h, c.red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    TRY(launch_change_norm(c, c.PhiPrev, c.red, c.siDelta, c.siDeltaPrev, learnEvery > 0));
+    double h[3];
+    UMT_CUDA(cudaMemcpyAsync(h, c.red, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     UMT_CUDA(cudaStreamSynchronize(c.stream));
     rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
-    const double rAbs = std::sqrt(h[0]);
+    const double rAbs = std::sqrt(h[2]);          // amplification-weighted change (learned guard)
     double dist = -1.0;                           // relative distance to phi_ref
     if (ref) {
-      TRY(launch_distance(c, ref, c.red + 2));
-      UMT_CUDA(cudaMemcpyAsync(h, c.red + 2, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+      TRY(launch_distance(c, ref, c.red + 8));
+      UMT_CUDA(cudaMemcpyAsync(h, c.red + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
       UMT_CUDA(cudaStreamSynchronize(c.stream));
       dist = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
     }
     if (pending) {
       // The sweep after a learned correction is its check: the correction
       // stays only if the iteration residual dropped below the one before it.
+      // The residual is weighted per zone and group by 1/(1 - c), the factor
+      // by which it understates the error where scattering dominates; an
+      // unweighted norm would reject corrections that remove slowly decaying
+      // error in thick scattering zones at the price of smaller, quickly
+      // damped errors in thin ones.
       pending = false;
       if (rAbs < rBefore) {
         ++kept;
@@ -1092,7 +1213,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
     // two plain iterations since the last correction give the change ratio
     if (learnEvery > 0 && it >= learnStart && plain >= std::max(learnEvery, 2)) {
       UMT_CUDA(cudaMemcpyAsync(c.siKeep, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
-      TRY(mlp_correct(c, c.siDelta, c.siDeltaPrev));
+      TRY(mlp_correct(c, c.Phi, c.siDelta, c.siDeltaPrev));
       UMT_CUDA(cudaMemcpyAsync(c.PhiPrev, c.Phi, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
       rBefore = rAbs;
       pending = true;
@@ -1103,12 +1224,14 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
     UMT_CUDA(cudaMemcpyAsync(c.Phi, c.siKeep, ncG * 8, cudaMemcpyDeviceToDevice, c.stream));
     ++rejected;
   }
-  if (learnEvery > 0) TRY(mlp_status());
+  if (learnEvery > 0 && !mixed) TRY(mlp_status());
+  if (prec == UMT_FP64) fp64Sweeps = sweeps;
   if (prm->save_psi) {
+    const int sp = mixed ? UMT_FP64 : prec;     // the mixed iterate is FP64-accurate
     TRY(launch_build_source(c, q));
-    TRY(launch_sweep_once(c, prec, true));
+    TRY(launch_sweep_once(c, sp, true));
     ++sweeps;
-    if (prec == UMT_FP64) c.cur64 = 1 - c.cur64; else c.cur32 = 1 - c.cur32;
+    if (sp == UMT_FP64) { c.cur64 = 1 - c.cur64; ++fp64Sweeps; } else c.cur32 = 1 - c.cur32;
   }
   UMT_CUDA(cudaEventRecord(t1, c.stream));
   UMT_CUDA(cudaStreamSynchronize(c.stream));
@@ -1119,6 +1242,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   res->grey_sweeps = greySweeps;
   res->learned_kept = kept;
   res->learned_rejected = rejected;
+  res->fp64_sweeps = fp64Sweeps;
   return conv ? 0 : set_error(UMT_ERR_NOTCONV, "not converged after %d iterations (rel change %.3e)", it, rel);
 }
 
@@ -1135,7 +1259,7 @@ int umt103_tally_precision(const double *siga, double speed_light, int precision
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   if (!t || !(speed_light > 0.0)) return set_error(UMT_ERR_ARG, "bad tally arguments");
-  if (!c.red) TRY(dalloc(&c.red, 8));
+  if (!c.red) TRY(dalloc(&c.red, 16));
   const size_t nzG = (size_t)c.nz * c.G;
   double *dsiga = nullptr;
   if (siga) {

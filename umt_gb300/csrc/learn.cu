@@ -762,7 +762,7 @@ bool mlp_ready_for(int G) { return g_mlp.ready && g_mlp.G == G; }
 
 // Zone features of the context's iterate, the network's multipliers, and
 // Phi += m * Delta on every corner (on the context's stream).
-int mlp_correct(Ctx &c, const double *Delta, const double *DeltaPrev) {
+int mlp_correct(Ctx &c, double *Target, const double *Delta, const double *DeltaPrev) {
   Mlp &n = g_mlp;
   if (!mlp_ready_for(c.G)) return set_error(UMT_ERR_STATE, "learned model: none for G=%d (umt103_mlp_init)", c.G);
   int rc = mlp_workspace(n, c.nz);
@@ -775,12 +775,12 @@ int mlp_correct(Ctx &c, const double *Delta, const double *DeltaPrev) {
     c.hMean = std::cbrt(vt / c.nz);
   }
   k_mlp_features<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, c.G, n.K1, c.hMean, c.numCorner, c.cOffSet, c.Volume,
-                                                           c.Sigt, c.SigS, c.Phi, Delta, DeltaPrev, n.X, nullptr,
+                                                           c.Sigt, c.SigS, Target, Delta, DeltaPrev, n.X, nullptr,
                                                            nullptr);
   UMT_CUDA(cudaGetLastError());
   rc = mlp_forward(n, c.nz, false, c.stream);
   if (rc) return rc;
-  k_mlp_apply<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.G, n.N4, c.cToZone, n.O, Delta, c.Phi);
+  k_mlp_apply<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.G, n.N4, c.cToZone, n.O, Delta, Target);
   UMT_CUDA(cudaGetLastError());
   return 0;
 }

@@ -48,22 +48,80 @@ __device__ void block_reduce_add(double (&v)[NV], double *out) {
   }
 }
 
-// sum (phi - prev)^2, sum phi^2; then prev = phi.  With delta given, the
-// change is kept too (deltaPrev, if given, receives the change before it).
-__global__ void k_change_norm(size_t n, const double *Phi, double *prev, double *out2, double *delta,
-                              double *deltaPrev) {
-  double v[2] = {0.0, 0.0};
+// Amplification weight of a zone and group: the infinite-medium factor
+// 1/(1 - c), c = sigma_s/sigma_t, by which source iteration's residual
+// understates its error where scattering dominates (capped at 1e3).
+__device__ __forceinline__ double amp_weight(const double *Sigt, const double *SigS, size_t zg) {
+  return 1.0 / fmax(1.0 - SigS[zg] / Sigt[zg], 1.0e-3);
+}
+
+// sum (phi - prev)^2, sum phi^2, and (with weights) sum (w (phi - prev))^2
+// into out[0], out[1], out[2]; then prev = phi.  With delta given, the change
+// is kept too (deltaPrev, if given, receives the change before it).
+__global__ void k_change_norm(size_t n, int G, const double *Phi, double *prev, double *out, double *delta,
+                              double *deltaPrev, const int *cToZone, const double *Sigt, const double *SigS) {
+  double v[3] = {0.0, 0.0, 0.0};
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const double d = Phi[i] - prev[i];
     v[0] += d * d;
     v[1] += Phi[i] * Phi[i];
+    if (cToZone) {
+      const int c = (int)(i / G), g = (int)(i - (size_t)c * G);
+      const double wd = amp_weight(Sigt, SigS, (size_t)cToZone[c] * G + g) * d;
+      v[2] += wd * wd;
+    }
     prev[i] = Phi[i];
     if (delta) {
       if (deltaPrev) deltaPrev[i] = delta[i];
       delta[i] = d;
     }
   }
+  block_reduce_add<3>(v, out);
+}
+
+// STotal = wtiso (sigma_s vec + q)
+__global__ void k_build_source_vec(int nc, int G, const int *cToZone, const double *sigs, const double *q,
+                                   const double *vec, double *STotal) {
+  const size_t n = (size_t)nc * G;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i / G), g = (int)(i - (size_t)c * G);
+    const size_t zg = (size_t)cToZone[c] * G + g;
+    STotal[i] = WTISO * (sigs[zg] * vec[i] + (q ? q[zg] : 0.0));
+  }
+}
+
+// R = Phi - X; out2 += {|R|^2, |Phi|^2}
+__global__ void k_residual(size_t n, const double *Phi, const double *X, double *R, double *out2) {
+  double v[2] = {0.0, 0.0};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double r = Phi[i] - X[i];
+    R[i] = r;
+    v[0] += r * r;
+    v[1] += Phi[i] * Phi[i];
+  }
   block_reduce_add<2>(v, out2);
+}
+
+// One step of the correction iteration D <- K D + R (Phi = K D from the
+// homogeneous sweep): d = (Phi + R) - D, D = Phi + R, the change history
+// shifted; out += {|d|^2, |D|^2, |w d|^2} (w: amp_weight)
+__global__ void k_inner_update(size_t n, int G, const double *Phi, const double *R, double *D, double *delta,
+                               double *deltaPrev, const int *cToZone, const double *Sigt, const double *SigS,
+                               double *out) {
+  double v[3] = {0.0, 0.0, 0.0};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double dn = Phi[i] + R[i];
+    const double d = dn - D[i];
+    D[i] = dn;
+    deltaPrev[i] = delta[i];
+    delta[i] = d;
+    const int c = (int)(i / G), g = (int)(i - (size_t)c * G);
+    const double wd = amp_weight(Sigt, SigS, (size_t)cToZone[c] * G + g) * d;
+    v[0] += d * d;
+    v[1] += dn * dn;
+    v[2] += wd * wd;
+  }
+  block_reduce_add<3>(v, out);
 }
 
 // sum (phi - ref)^2, sum ref^2
@@ -278,17 +336,41 @@ int launch_build_source(Ctx &c, const double *q) {
   return 0;
 }
 
-int launch_change_norm(Ctx &c, double *prev, double *out2, double *delta, double *deltaPrev) {
+int launch_change_norm(Ctx &c, double *prev, double *out3, double *delta, double *deltaPrev, bool weighted) {
   const size_t n = (size_t)c.nc * c.G;
-  UMT_CUDA(cudaMemsetAsync(out2, 0, 2 * sizeof(double), c.stream));
-  k_change_norm<<<152 * 4, 256, 0, c.stream>>>(n, c.Phi, prev, out2, delta, deltaPrev);
+  UMT_CUDA(cudaMemsetAsync(out3, 0, 3 * sizeof(double), c.stream));
+  k_change_norm<<<152 * 4, 256, 0, c.stream>>>(n, c.G, c.Phi, prev, out3, delta, deltaPrev,
+                                               weighted ? c.cToZone : nullptr, c.Sigt, c.SigS);
   UMT_CUDA(cudaGetLastError());
   return 0;
 }
 
-int launch_distance(Ctx &c, const double *ref, double *out2) {
+int launch_distance(Ctx &c, const double *ref, double *out2, const double *x) {
   UMT_CUDA(cudaMemsetAsync(out2, 0, 2 * sizeof(double), c.stream));
-  k_distance<<<152 * 4, 256, 0, c.stream>>>((size_t)c.nc * c.G, c.Phi, ref, out2);
+  k_distance<<<152 * 4, 256, 0, c.stream>>>((size_t)c.nc * c.G, x ? x : c.Phi, ref, out2);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int launch_build_source_vec(Ctx &c, const double *vec, const double *q) {
+  const size_t n = (size_t)c.nc * c.G;
+  k_build_source_vec<<<(int)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, c.stream>>>(
+      c.nc, c.G, c.cToZone, c.SigS, q, vec, c.STotal);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int launch_residual(Ctx &c, const double *X, double *R, double *out2) {
+  UMT_CUDA(cudaMemsetAsync(out2, 0, 2 * sizeof(double), c.stream));
+  k_residual<<<152 * 4, 256, 0, c.stream>>>((size_t)c.nc * c.G, c.Phi, X, R, out2);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int launch_inner_update(Ctx &c, const double *R, double *D, double *delta, double *deltaPrev, double *out3) {
+  UMT_CUDA(cudaMemsetAsync(out3, 0, 3 * sizeof(double), c.stream));
+  k_inner_update<<<152 * 4, 256, 0, c.stream>>>((size_t)c.nc * c.G, c.G, c.Phi, R, D, delta, deltaPrev, c.cToZone,
+                                                c.Sigt, c.SigS, out3);
   UMT_CUDA(cudaGetLastError());
   return 0;
 }

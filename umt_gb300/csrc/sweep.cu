@@ -427,6 +427,8 @@ void invalidate_graphs(Ctx &c) {
       if (c.graphs[i][j]) { cudaGraphExecDestroy(c.graphs[i][j]); c.graphs[i][j] = nullptr; }
   for (auto &g : c.graphsWT)
     if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+  for (auto &g : c.graphsH)
+    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
   for (auto &a : c.siGraph)
     for (auto &b : a)
       for (auto &g : b)
@@ -438,7 +440,8 @@ void invalidate_graphs(Ctx &c) {
 // sweeps replay it with a single launch.
 static int sweep_via_graph(Ctx &c, int precision) {
   const int cur = precision == 0 ? c.cur64 : c.cur32;
-  cudaGraphExec_t &ex = (precision == 1 && c.wantExitsThrough) ? c.graphsWT[cur] : c.graphs[precision][cur];
+  cudaGraphExec_t &ex = (precision == 1 && c.homog32) ? c.graphsH[cur]
+                        : (precision == 1 && c.wantExitsThrough) ? c.graphsWT[cur] : c.graphs[precision][cur];
   if (!ex) {
     cudaGraph_t gr = nullptr;
     UMT_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));

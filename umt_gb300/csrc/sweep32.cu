@@ -458,8 +458,8 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   p.items2 = c.sch.items2; p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
   p.order = c.sch.order;
   p.rec = (const float4 *)c.rec32; p.conn = (const int4 *)c.conn32;
-  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
-  p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
+  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = c.homog32 ? 0.f : (float)c.tau;
+  p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.homog32 ? c.psiB32h : c.psiB32;
   const int TEAMS = 128 / GT;
   const size_t smem = (size_t)2 * TEAMS * p.stride * sizeof(float);
   PersistP q;

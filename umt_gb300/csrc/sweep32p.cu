@@ -705,8 +705,8 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   p.bstride = blob_stride_p(c.progMaxChunks);
   p.hdr = (const uint4 *)c.hdr32; p.prog = (const uint4 *)c.prog32;
   p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
-  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = (float)c.tau;
-  p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.psiB32;
+  p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = c.homog32 ? 0.f : (float)c.tau;
+  p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.homog32 ? c.psiB32h : c.psiB32;
   p.psibOut = c.psibOut;
   const int TEAMS = P32_NT / GT;
   const size_t smem = (size_t)TEAMS * ((size_t)p.tstride * 4 + p.bstride);

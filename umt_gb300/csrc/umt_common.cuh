@@ -100,6 +100,12 @@ struct Ctx {
   cudaGraphExec_t siGraph[2][2][2] = {};        // [precision][cur][with phi_ref]
   bool inSIGraph = false;                       // enqueueing into that graph's body (no event records)
   int siGraphState = 0;                         // 0 untried, 1 works, -1 unavailable (host loop)
+  // homogeneous FP32 sweeps (no tau*psi_old term, no boundary inflow): the
+  // inner solves of mixed-precision source iteration
+  bool homog32 = false;
+  float *psiB32h = nullptr;                     // boundary rows of those sweeps (incoming rows stay zero)
+  cudaGraphExec_t graphsH[2] = {nullptr, nullptr};
+  double *mixX = nullptr, *mixR = nullptr, *mixD = nullptr;   // [nc][G] outer iterate, residual, correction
   double *red = nullptr;                        // [8] reduction slots
   // angular flux, double buffered: psi[cur] = saved Psi, psi[1-cur] = new
   double *psi64[2] = {nullptr, nullptr};
@@ -171,13 +177,19 @@ int record_mid(Ctx &c);
 int launch_convert_source(Ctx &c);
 // source iteration and edits (si.cu)
 int launch_build_source(Ctx &c, const double *q);
-int launch_change_norm(Ctx &c, double *prev, double *out2, double *delta = nullptr, double *deltaPrev = nullptr);
+// out3[0..2] = |change|^2, |phi|^2, |amplification-weighted change|^2 (the
+// last only with weighted); out3 needs three slots
+int launch_change_norm(Ctx &c, double *prev, double *out3, double *delta = nullptr, double *deltaPrev = nullptr,
+                       bool weighted = false);
 // learned correction (learn.cu)
 bool mlp_ready_for(int G);
-int mlp_correct(Ctx &c, const double *Delta, const double *DeltaPrev);
+int mlp_correct(Ctx &c, double *Target, const double *Delta, const double *DeltaPrev);
 int mlp_status();
 int launch_energy(Ctx &c, const double *siga_dev, int precision, double *out4);
-int launch_distance(Ctx &c, const double *ref, double *out2);
+int launch_distance(Ctx &c, const double *ref, double *out2, const double *x = nullptr);
+int launch_build_source_vec(Ctx &c, const double *vec, const double *q);
+int launch_residual(Ctx &c, const double *X, double *R, double *out2);
+int launch_inner_update(Ctx &c, const double *R, double *D, double *delta, double *deltaPrev, double *out3);
 // grey transport acceleration (si.cu)
 int gta_prepare(Ctx &c);
 int gta_apply(Ctx &c, const double *x, double wR);
