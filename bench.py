@@ -267,6 +267,43 @@ def time_to_converge(lib, prob, use_gta=False, tol64=1e-8, tol32=1e-7):
             "tolerance_fp64": tol64, "tolerance_fp32": tol32}
 
 
+def ttc_learned(args, lib):
+    """Time to converge on the strongly scattering distribution (config 5:
+    sigma_t log-uniform on [1, 1e3], c in [0.95, 0.999], 32 groups, 128
+    directions), on a reduced mesh of --ttc-tiles tiles per axis, where plain
+    FP64 source iteration still finishes in about a minute.  The learned
+    correction is first trained on the device from seeded problems of 3 and
+    4 tiles per axis (each solved by FP64 sweeps under GMRES); then every
+    method iterates from zero until PhiTotal is within 1e-6 relative L2 of
+    the FP64 GMRES answer (checked on the device after each iteration)."""
+    from umt_gb300 import capi, learned
+    t0 = time.perf_counter()
+    train = [learned.strongly_scattering_problem(3 + (k % 2), seed=5000 + k) for k in range(8)]
+    summary = learned.train_on_problems(lib, train, steps=1500, batch=4096, lr=2e-3)
+    summary["wall_s"] = time.perf_counter() - t0
+    prob = learned.strongly_scattering_problem(args.ttc_tiles, seed=5)
+    learned.load_problem(lib, prob, flags=3 | 8)
+    t1 = time.perf_counter()
+    phi_star, n_ref = learned.converged_phi(lib, prob)
+    ref_s = time.perf_counter() - t1
+    runs = {}
+    for name, prec, le in (("fp64_plain", capi.UMT_FP64, 0), ("fp64_learned", capi.UMT_FP64, 5),
+                           ("fp32_plain", capi.UMT_FP32, 0), ("mixed_plain", capi.UMT_MIXED, 0),
+                           ("mixed_learned", capi.UMT_MIXED, 5)):
+        r = learned.iterate_to(lib, prob, phi_star, precision=prec, learn_every=le, learn_start=3,
+                               max_iters=4000 if prec != capi.UMT_MIXED else 60)
+        runs[name] = {k: r[k] for k in ("iterations", "sweeps", "fp64_sweeps", "seconds", "wall_s", "error",
+                                         "converged", "learned_kept", "learned_rejected")}
+    base = runs["fp64_plain"]["seconds"]
+    best = runs["mixed_learned"]
+    return {"workload": f"strongly scattering, {args.ttc_tiles}^3 tiles ({prob.mesh.nzones} zones), 128 directions, "
+                        f"32 groups, seed 5", "target": "1e-6 relative L2 of PhiTotal vs FP64 GMRES (1e-10)",
+            "reference_fp64_sweeps": n_ref, "reference_s": ref_s, "training": summary, "runs": runs,
+            "speedup_mixed_learned_vs_fp64_plain": base / best["seconds"] if best["converged"] else None,
+            "speedup_fp64_learned_vs_fp64_plain": base / runs["fp64_learned"]["seconds"],
+            "time": "device seconds of umt103_source_iterate (CUDA events); wall_s is the host time of the call"}
+
+
 def run_rz(args):
     """2-D RZ sweep (--precision, FP32 by default): nr x nz quadrilaterals,
     RZ product quadrature P = 4, Az = 8 (144 directions), 16 groups.  Device
@@ -470,6 +507,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 same-workload sweep figure")
+    ap.add_argument("--no-learned", action="store_true", help="--config 5: skip the learned time-to-converge leg")
+    ap.add_argument("--ttc-tiles", type=int, default=6, help="--config 5: tiles per axis of the time-to-converge mesh")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
     ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (precision as --precision)")
     ap.add_argument("--rz-cells", type=int, default=200, help="RZ mesh: cells per direction")
@@ -624,6 +663,8 @@ def main():
         line["fp64"] = fp64_sweep_figure(lib, prob, units)
     if world == 1 and not args.no_ttc:
         line["time_to_converge"] = time_to_converge(lib, prob, use_gta=args.gta)
+    if world == 1 and args.config == 5 and not args.no_learned:
+        line["time_to_converge"] = ttc_learned(args, lib)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_sample(prob)
     print(json.dumps(line), flush=True)

@@ -371,6 +371,19 @@ int umt103_last_timing(double *out3);
  * (gpu/GPU_SweepUCBxyz.cu:30-31). */
 int umt103_set_group_tile(int lanes_per_zone, int groups_per_lane);
 
+/* Autotuner (no reference counterpart): times every group tile the FP32
+ * sweep supports on the current context's problem (reps timed sweeps after
+ * one that captures the graph; the sweeps overwrite PhiTotal), keeps the
+ * fastest, and caches it for the problem's shape (groups, directions, zones,
+ * corners, sweep mode).  times (may be NULL) receives up to max_times
+ * triples {lanes_per_zone, groups_per_lane, best ms}; *ntimes their count.
+ * umt103_autotune_contexts tunes each listed context whose shape has no
+ * cached tile and applies the cached tile to the others; umt103_batch_sweep
+ * applies the cached tile of their shape to contexts with no tile set. */
+int umt103_autotune(int reps, int *lanes_per_zone, int *groups_per_lane, double *times, int max_times,
+                    int *ntimes);
+int umt103_autotune_contexts(const int *ids, int n, int reps);
+
 /* FP32 sweep kernel and scheduling.  Modes 0 and 2 launch one kernel per
  * dependency stage (the hyperplane loop of snac/SweepUCBxyz.F90:103, all
  * directions at once):

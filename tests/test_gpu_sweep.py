@@ -304,3 +304,46 @@ def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):
     assert np.array_equal(out[0][1], out[1][1])
     assert np.array_equal(out[0][2], out[1][2])
     assert not np.array_equal(out[1][1], PsiB0)                   # exits were written back
+
+
+def test_autotuner_picks_the_fastest_tile_and_keeps_results(umtlib):
+    """umt103_autotune times every group tile, keeps the fastest, and the
+    tuned sweep equals a sweep with that tile set by hand (bit for bit) and
+    the FP64 sweep within the FP32 tolerance; contexts of the same shape in a
+    batch take the cached tile."""
+    from umt_gb300.problems import synthetic_problem as sp
+    prob = sp((4, 4, 3), 4, 4, 16, seed=7, time_dependent=True)
+    m = prob.mesh
+    st = np.repeat(prob.q_ext, m.numCorner, axis=0) / (4 * np.pi)
+    umtlib.init(m, prob.omega, prob.weight, prob.ngr, flags=3 | 8)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    umtlib.set_source(st)
+    best, times = umtlib.autotune(reps=2)
+    assert set(times) == {(16, 1), (8, 2), (4, 4)}
+    assert best == min(times, key=times.get)
+    umtlib.sweep_resident(False, capi.UMT_FP32)
+    tuned = umtlib.get_phi()
+    umtlib.set_group_tile(*best)
+    umtlib.sweep_resident(False, capi.UMT_FP32)
+    assert np.array_equal(umtlib.get_phi(), tuned)
+    umtlib.sweep_resident(False, capi.UMT_FP64)
+    assert rel_err(tuned, umtlib.get_phi()) < 1e-5
+    ids = []
+    for _ in range(2):
+        cid = umtlib.context_create()
+        umtlib.context_select(cid)
+        umtlib.init(m, prob.omega, prob.weight, prob.ngr, flags=2 | 8)
+        umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+        umtlib.set_psi(prob.psi0, None)
+        umtlib.set_source(st)
+        ids.append(cid)
+    umtlib.context_select(0)
+    umtlib.autotune_contexts(ids)                     # the shape is cached: no timing
+    umtlib.batch_sweep(ids, capi.UMT_FP32)
+    for cid in ids:
+        umtlib.context_select(cid)
+        assert np.array_equal(umtlib.get_phi(m.ncornr, prob.ngr), tuned)
+    umtlib.context_select(0)
+    for cid in ids:
+        umtlib.context_destroy(cid)

@@ -1,43 +1,30 @@
-"""Group-tile autotuner for the FP32 sweep.
+"""Group-tile autotuner for the FP32 sweep (host face of umt103_autotune).
 
-The production kernel assigns one team of `lanes_per_zone` lanes to each
-(direction, zone) pair and gives every lane `groups_per_lane` consecutive
-groups (lanes_per_zone * groups_per_lane = G).  More groups per lane amortise
-the zone's structure decode and widen every load to 64 or 128 bits, but raise
-register use (about 96 / 124 / 200 registers per thread for 1 / 2 / 4 groups
-per lane) and lower the number of resident teams.  The best point depends on G,
-the direction count and the mesh, so it is measured: every legal tile is timed
-on the problem already loaded in the library, and the fastest is kept.
+The sweep assigns one team of `lanes_per_zone` lanes to each (direction,
+zone) pair and gives every lane `groups_per_lane` consecutive groups
+(lanes_per_zone * groups_per_lane = G).  More groups per lane amortise the
+zone program's decode and widen every load, but raise register use and lower
+the number of resident teams; the best point depends on G, the direction
+count and the mesh, so the library times every legal tile on the loaded
+problem, keeps the fastest and caches it per problem shape
+(umt_gb300/csrc/capi.cu, umt103_autotune / umt103_autotune_contexts).
 """
 from __future__ import annotations
 
 from . import capi
 
-LANES = (1, 2, 4, 8, 16, 32)
-GROUPS_PER_LANE = (1, 2, 4)
+
+def autotune(lib: capi.Library, reps: int = 2, verbose: bool = False):
+    """Tune the current context.  Returns (best_tile, {tile: ms})."""
+    best, times = lib.autotune(reps)
+    if verbose:
+        for (gt, gpl), ms in sorted(times.items()):
+            print(f"tile lanes_per_zone={gt:2d} groups_per_lane={gpl}: {ms:.3f} ms")
+    return best, times
 
 
-def candidates(G: int):
-    return [(G // gpl, gpl) for gpl in GROUPS_PER_LANE if G % gpl == 0 and (G // gpl) in LANES]
-
-
-def autotune(lib: capi.Library, reps: int = 3, verbose: bool = False):
-    """Time every legal tile with device-resident sweeps; keep the fastest.
-
-    Returns (best_tile, {tile: stage-kernel ms})."""
-    results = {}
-    for tile in candidates(lib.G):
-        lib.set_group_tile(*tile)
-        lib.sweep_resident(False, capi.UMT_FP32)          # capture + warm
-        best = float("inf")
-        for _ in range(reps):
-            lib.sweep_resident(False, capi.UMT_FP32)
-            best = min(best, lib.timing()[1])
-        results[tile] = best
-        if verbose:
-            print(f"tile lanes_per_zone={tile[0]:2d} groups_per_lane={tile[1]}: {best:.3f} ms")
-    if not results:
-        return None, results
-    best_tile = min(results, key=results.get)
-    lib.set_group_tile(*best_tile)
-    return best_tile, results
+def autotune_batch(lib: capi.Library, ids, reps: int = 2):
+    """Tune each distinct problem shape of a batch of contexts once; every
+    context then sweeps with its shape's tile (umt103_batch_sweep applies
+    them)."""
+    lib.autotune_contexts(ids, reps)

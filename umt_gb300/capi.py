@@ -101,7 +101,8 @@ def load():
                   "umt103_batch_sweep", "umt103_psib_rows", "umt103_hold_item",
                   "umt103_mlp_init", "umt103_mlp_info", "umt103_mlp_get_params", "umt103_mlp_set_params",
                   "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect", "umt103_mlp_set_targets",
-                  "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train"):
+                  "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train", "umt103_autotune",
+                  "umt103_autotune_contexts"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_mlp_finalize.restype = None
         _fp = C.POINTER(C.c_float)
@@ -128,7 +129,8 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_get_geometry_rz", "umt103_psib_rows", "umt103_hold_item",
             "umt103_mlp_init", "umt103_mlp_finalize", "umt103_mlp_info", "umt103_mlp_get_params",
             "umt103_mlp_set_params", "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect",
-            "umt103_mlp_set_targets", "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train"]
+            "umt103_mlp_set_targets", "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train",
+            "umt103_autotune", "umt103_autotune_contexts"]
 
 
 def check(rc):
@@ -361,6 +363,17 @@ class Library:
 
     def set_group_tile(self, lanes_per_zone, groups_per_lane):
         check(self.lib.umt103_set_group_tile(int(lanes_per_zone), int(groups_per_lane)))
+
+    def autotune(self, reps=2):
+        """umt103_autotune: ((lanes_per_zone, groups_per_lane), {tile: best ms})."""
+        gt, gpl, nt = C.c_int(0), C.c_int(0), C.c_int(0)
+        times = np.zeros((8, 3))
+        check(self.lib.umt103_autotune(int(reps), C.byref(gt), C.byref(gpl), _d(times), 8, C.byref(nt)))
+        return (gt.value, gpl.value), {(int(t[0]), int(t[1])): float(t[2]) for t in times[:nt.value]}
+
+    def autotune_contexts(self, ids, reps=2):
+        arr = (C.c_int * len(ids))(*ids)
+        check(self.lib.umt103_autotune_contexts(arr, len(ids), int(reps)))
 
     def set_gta(self, max_krylov=10, tol=1e-4, spectrum=0):
         self.lib.umt103_set_gta.argtypes = [C.c_int, C.c_double, C.c_int]

@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstring>
 #include <algorithm>
+#include <map>
 
 namespace umt {
 
@@ -158,6 +159,101 @@ static void drop_batch_graph(size_t k) {
   g_batch.erase(g_batch.begin() + (long)k);
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: the FP32 sweep's group tile (lanes per (direction, zone) pair x
+// groups per lane) timed on the loaded problem, the fastest kept, and cached
+// per problem shape (groups, directions, zones, corners, sweep mode) for
+// every context of the process.
+// ---------------------------------------------------------------------------
+struct TileKey {
+  int G, A, nz, nc, mode;
+  bool operator<(const TileKey &o) const {
+    if (G != o.G) return G < o.G;
+    if (A != o.A) return A < o.A;
+    if (nz != o.nz) return nz < o.nz;
+    if (nc != o.nc) return nc < o.nc;
+    return mode < o.mode;
+  }
+};
+static std::map<TileKey, std::pair<int, int>> g_tiles;
+
+static TileKey tile_key(const Ctx &c) { return TileKey{c.G, c.A, c.nz, c.nc, c.sweepMode}; }
+
+// A context with no tile of its own takes the tuned tile of its shape.
+static void apply_cached_tile(Ctx &c) {
+  if (c.tileGT != 0) return;
+  auto it = g_tiles.find(tile_key(c));
+  if (it == g_tiles.end()) return;
+  invalidate_graphs(c);
+  c.tileGT = it->second.first;
+  c.tileGPL = it->second.second;
+}
+
+static int autotune_ctx(Ctx &c, int reps, double *times, int maxTimes, int *ntimes) {
+  if (!c.psi32[0]) return set_error(UMT_ERR_STATE, "autotune: the context has no FP32 flux");
+  if (c.rz) return set_error(UMT_ERR_STATE, "autotune: RZ contexts are not tuned");
+  reps = std::max(reps, 1);
+  double best = 1e300;
+  int bGT = 0, bGPL = 0, k = 0;
+  for (int gpl : {1, 2, 4}) {
+    if (c.G % gpl) continue;
+    const int gt = c.G / gpl;
+    if (!sweep32_supported(c.G, gt, gpl)) continue;
+    invalidate_graphs(c);
+    c.tileGT = gt; c.tileGPL = gpl;
+    double t = 1e300;
+    for (int r = 0; r <= reps; ++r) {                  // the first sweep captures the graph
+      UMT_CUDA(cudaEventRecord(c.ev0, c.stream));
+      TRY(launch_sweep_once(c, UMT_FP32, true));
+      UMT_CUDA(cudaEventRecord(c.ev1, c.stream));
+      UMT_CUDA(cudaStreamSynchronize(c.stream));
+      float ms = 0.f;
+      UMT_CUDA(cudaEventElapsedTime(&ms, c.ev0, c.ev1));
+      if (r > 0) t = std::min(t, (double)ms);
+    }
+    if (times && k < maxTimes) { times[3 * k] = gt; times[3 * k + 1] = gpl; times[3 * k + 2] = t; }
+    ++k;
+    if (t < best) { best = t; bGT = gt; bGPL = gpl; }
+  }
+  if (ntimes) *ntimes = k;
+  if (!bGT) return set_error(UMT_ERR_ARG, "autotune: no group tile covers G=%d", c.G);
+  invalidate_graphs(c);
+  c.tileGT = bGT; c.tileGPL = bGPL;
+  g_tiles[tile_key(c)] = {bGT, bGPL};
+  return 0;
+}
+
+int umt103_autotune(int reps, int *lanes_per_zone, int *groups_per_lane, double *times, int max_times,
+                    int *ntimes) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  TRY(autotune_ctx(c, reps, times, max_times, ntimes));
+  if (lanes_per_zone) *lanes_per_zone = c.tileGT;
+  if (groups_per_lane) *groups_per_lane = c.tileGPL;
+  return 0;
+}
+
+int umt103_autotune_contexts(const int *ids, int n, int reps) {
+  if (!ids || n <= 0) return set_error(UMT_ERR_ARG, "no contexts");
+  Ctx *keep = g_cur;
+  int rc = 0;
+  for (int k = 0; k < n && !rc; ++k) {
+    const int id = ids[k];
+    if (id < 0 || id >= (int)g_ctx.size() || !g_ctx[id] || !g_ctx[id]->ready) {
+      rc = set_error(UMT_ERR_ARG, "autotune: context %d not initialised", id);
+      break;
+    }
+    Ctx &c = *g_ctx[id];
+    g_cur = &c;
+    c.tileGT = 0;
+    c.tileGPL = 0;
+    if (g_tiles.count(tile_key(c))) apply_cached_tile(c);
+    else rc = autotune_ctx(c, reps, nullptr, 0, nullptr);
+  }
+  g_cur = keep;
+  return rc;
+}
+
 int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
   if (!ids || n <= 0) return set_error(UMT_ERR_ARG, "empty batch");
   if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
@@ -179,9 +275,11 @@ int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
   }
   Ctx *keep = g_cur;
   int rc = 0;
-  // one-time preparation of each context (outside any capture), then the key
+  // tuned tiles of each context's shape, one-time preparation of each
+  // context (outside any capture), then the key
   for (int k = 0; k < n && !rc; ++k) {
     g_cur = g_ctx[ids[k]];
+    if (precision == UMT_FP32) apply_cached_tile(*g_cur);
     bool prog = false;
     if (precision == UMT_FP32) rc = fp32_program_path(*g_cur, &prog);
   }
