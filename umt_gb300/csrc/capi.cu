@@ -68,10 +68,11 @@ static void free_ctx(Ctx &c) {
   dfree(s.items); dfree(s.items2); dfree(s.stageCount); dfree(s.stageOffset); dfree(s.need); dfree(s.exitMask);
   dfree(s.needInit); dfree(c.dep); dfree(c.ticket);
   dfree(s.bad); dfree(s.order); dfree(s.level); dfree(s.nHyper); dfree(s.processed);
+  dfree(s.cycZ); dfree(s.cycRow); dfree(c.cycPsi64); dfree(c.cycPsi32);
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red); dfree(c.siDelta); dfree(c.siDeltaPrev); dfree(c.siKeep);
   dfree(c.siState); dfree(c.siRef); dfree(c.psiB32h); dfree(c.mixX); dfree(c.mixR); dfree(c.mixD);
-  dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS);
+  dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS); dfree(c.gtaZ);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
   dfree(c.psibOut); dfree(c.phiOut);
@@ -534,7 +535,7 @@ static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int fla
   TRY(dalloc(&s.need, nAZ)); TRY(dalloc(&s.exitMask, (nAZ + 3) & ~(size_t)3)); TRY(dalloc(&s.bad, nAZ));
   TRY(dalloc(&s.needInit, nAZ)); TRY(dalloc(&c.dep, nAZ)); TRY(dalloc(&c.ticket, 1));
   TRY(dalloc(&s.order, nAZ)); TRY(dalloc(&s.level, nAZ)); TRY(dalloc(&s.nHyper, A));
-  TRY(dalloc(&s.processed, 1));
+  TRY(dalloc(&s.processed, 1)); TRY(dalloc(&s.cycZ, nAZ));
   TRY(build_schedule(c));
 
   // ---- state ----
@@ -556,6 +557,7 @@ static int init_ctx(Ctx &c, const UmtMesh *m, const UmtQuad *q, int ngr, int fla
     TRY(dalloc(&c.psibOut, 1)); UMT_CUDA(cudaMemset(c.psibOut, 0, sizeof(double *)));
     TRY(dalloc(&c.phiOut, 1)); UMT_CUDA(cudaMemset(c.phiOut, 0, sizeof(double *)));
   }
+  TRY(cycle_from_psi(c));
   UMT_CUDA(cudaDeviceSynchronize());
   c.ready = true;
   return 0;
@@ -643,6 +645,7 @@ int umt103_set_psi(const double *Psi, const double *PsiB) {
   int rc = put(Psi, psiN, c.psi64[c.cur64], c.psi32[c.cur32]);
   if (!rc) rc = put(PsiB, psiBN, c.psiB64, c.psiB32);
   cudaFree(tmp);
+  if (!rc) rc = cycle_from_psi(c);               // the cycle list starts from the saved flux
   return rc;
 }
 
@@ -875,6 +878,8 @@ int umt103_set_sweep_mode(int mode) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   if (mode < 0 || mode > 2) return set_error(UMT_ERR_ARG, "sweep mode must be 0, 1 or 2");
+  if (mode == 1 && c.sch.nCyc > 0)
+    return set_error(UMT_ERR_CYCLE, "the persistent sweep (mode 1) does not run meshes with a cycle list");
   if (c.sweepMode != mode) invalidate_graphs(c);
   c.sweepMode = mode;
   return 0;
@@ -906,7 +911,8 @@ int umt103_schedule_info(int angle, int *nHyperPlanes, int *numCycles) {
   int h = 0;
   UMT_CUDA(cudaMemcpy(&h, c.sch.nHyper + angle, sizeof(int), cudaMemcpyDeviceToHost));
   if (nHyperPlanes) *nHyperPlanes = h;
-  if (numCycles) *numCycles = 0;
+  if (numCycles)
+    *numCycles = c.sch.hCycOff.empty() ? 0 : (int)(c.sch.hCycOff[angle + 1] - c.sch.hCycOff[angle]);
   return 0;
 }
 
@@ -928,59 +934,97 @@ int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume) {
   return 0;
 }
 
-// BiCGStab solve of the grey correction (rt/GTASolver.F90:219-402 structure:
-// two grey sweeps per iteration) followed by phi_g += chi_g eps.  Vectors are
-// FP64 on the device; slots of c.gtaVec: 0 x, 1 r, 2 rhat, 3 p, 4 v, 5 s, 6 t, 7 R.
-static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps) {
-  Ctx &q = *c.gta;
+// The grey correction of rt/GTASolver.F90:42-425 (the BiCGStab branch with
+// GreySweep, rt/GreySweep.F90): A = I - M with M the grey operator (grey S2
+// sweep plus stretched-TSA sweep, gta_op); the initial residual is M applied
+// to the grey source alone; inner products are weighted by sigma_s,grey V
+// (scat_prod) and the shadow product is their plain sum (scat_prod1); the
+// iteration stops when the zone-averaged correction changes by less than
+// tol relative to the zone energy plus correction (pointwise and L2), or
+// after max_krylov iterations.  Then phi_g += chi_g x (rt/addGreyCorrections.F90).
+// Vectors (FP64, device) in c.gtaVec: 0 x (GreyCorrection), 1 r, 3 d, 4 Ad,
+// 5 As, 7 R (grey source).  apply=false leaves PhiTotal unchanged.
+static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps, bool apply = true) {
   const int n = c.nc;
   double *V = c.gtaVec;
-  double *x = V, *r = V + (size_t)n, *rh = V + 2 * (size_t)n, *p = V + 3 * (size_t)n, *v = V + 4 * (size_t)n,
-         *s = V + 5 * (size_t)n, *t = V + 6 * (size_t)n;
+  double *x = V, *r = V + (size_t)n, *d = V + 3 * (size_t)n, *Ad = V + 4 * (size_t)n, *As = V + 5 * (size_t)n;
+  const double small = 1.0e-150;                  // adqtSmall, mods/constant_mod.F90:51
   TRY(gta_prepare(c));
-  // A y = y - K y, with K y = one grey sweep of the source wtiso*sigma_s,grey*y
-  auto applyA = [&](const double *y, double *out) -> int {
-    TRY(gta_apply(c, y, 0.0));
-    ++*greySweeps;
-    return gta_axpbypcz(c, n, 1.0, y, 0.0, out, -1.0, q.Phi);
-  };
-  TRY(gta_apply(c, nullptr, 1.0));                 // b = K0 R
-  ++*greySweeps;
   UMT_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, c.stream));
-  UMT_CUDA(cudaMemsetAsync(p, 0, (size_t)n * 8, c.stream));
-  UMT_CUDA(cudaMemsetAsync(v, 0, (size_t)n * 8, c.stream));
-  UMT_CUDA(cudaMemcpyAsync(r, q.Phi, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
-  UMT_CUDA(cudaMemcpyAsync(rh, q.Phi, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
+  TRY(gta_op(c, nullptr, r, true));               // CGResidual: M with the grey source, from zero
+  *greySweeps += 2;
+  UMT_CUDA(cudaMemcpyAsync(d, r, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
   double h[2];
-  TRY(gta_dot2(c, n, r, r, nullptr, nullptr, h));
-  const double bnorm = std::sqrt(h[0]);
-  if (!(bnorm > 0.0)) return 0;
-  double rho_old = 1.0, alpha = 1.0, omega = 1.0;
-  for (int it = 0; it < maxit; ++it) {
-    TRY(gta_dot2(c, n, rh, r, nullptr, nullptr, h));
-    const double rho = h[0];
-    if (std::fabs(rho) < 1e-300) break;
-    const double beta = (rho / rho_old) * (alpha / omega);
-    TRY(gta_axpbypcz(c, n, 1.0, r, beta, p, -beta * omega, v));       // p = r + beta (p - omega v)
-    TRY(applyA(p, v));
-    TRY(gta_dot2(c, n, rh, v, nullptr, nullptr, h));
-    if (std::fabs(h[0]) < 1e-300) break;
-    alpha = rho / h[0];
-    TRY(gta_axpbypcz(c, n, 1.0, r, 0.0, s, -alpha, v));              // s = r - alpha v
-    TRY(applyA(s, t));
-    TRY(gta_dot2(c, n, t, s, t, t, h));
-    if (!(h[1] > 0.0)) {
-      TRY(gta_axpbypcz(c, n, alpha, p, 1.0, x, 0.0, nullptr));
+  TRY(gta_sdot2(c, r, nullptr, nullptr, nullptr, h));
+  double rrOld = h[0];
+  int nGrey = 1;
+  for (int it = 0;; ++it) {
+    if (std::fabs(rrOld) < small) {
+      if (nGrey <= 2) UMT_CUDA(cudaMemcpyAsync(x, r, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
       break;
     }
-    omega = h[0] / h[1];
-    TRY(gta_axpbypcz(c, n, alpha, p, 1.0, x, omega, s));              // x += alpha p + omega s
-    TRY(gta_axpbypcz(c, n, 1.0, s, 0.0, r, -omega, t));               // r = s - omega t
-    rho_old = rho;
-    TRY(gta_dot2(c, n, r, r, nullptr, nullptr, h));
-    if (std::sqrt(h[0]) < tol * bnorm || omega == 0.0) break;
+    nGrey += 2;
+    TRY(gta_op(c, d, Ad, false));                 // Ad = d - M d
+    *greySweeps += 2;
+    TRY(gta_axpbypcz(c, n, 1.0, d, -1.0, Ad, 0.0, nullptr));
+    TRY(gta_sdot2(c, Ad, nullptr, nullptr, nullptr, h));
+    const double dAd = h[0];
+    if (std::fabs(dAd) < small) break;
+    const double alpha = rrOld / dAd;
+    TRY(gta_axpbypcz(c, n, -alpha, Ad, 1.0, r, 0.0, nullptr));          // r -= alpha Ad
+    TRY(gta_op(c, r, As, false));                 // As = r - M r
+    *greySweeps += 2;
+    TRY(gta_axpbypcz(c, n, 1.0, r, -1.0, As, 0.0, nullptr));
+    TRY(gta_sdot2(c, As, r, As, As, h));
+    const double omegaNum = h[0], omegaDen = h[1];
+    if (std::fabs(omegaDen) < small || std::fabs(omegaNum) < small) {
+      TRY(gta_axpbypcz(c, n, alpha, d, 1.0, x, 0.0, nullptr));
+      break;
+    }
+    const double omega = omegaNum / omegaDen;
+    TRY(gta_axpbypcz(c, n, alpha, d, 1.0, x, omega, r));                // x += alpha d + omega r
+    TRY(gta_axpbypcz(c, n, -omega, As, 1.0, r, 0.0, nullptr));         // r -= omega As
+    TRY(gta_sdot2(c, r, nullptr, nullptr, nullptr, h));
+    const double rr = h[0];
+    const double beta = (rr * alpha) / (rrOld * omega);
+    TRY(gta_axpbypcz(c, n, 1.0, r, beta, d, -beta * omega, Ad));       // d = r + beta (d - omega Ad)
+    double rel = 0.0;
+    TRY(gta_converge(c, x, &rel));
+    if (rel < tol || it + 1 >= maxit) break;
+    rrOld = rr;
   }
-  return gta_correct(c, x);
+  return apply ? gta_correct(c, x) : 0;
+}
+
+static int gta_alloc(Ctx &c) {
+  if (!c.gta) return set_error(UMT_ERR_STATE, "GTA context not created (init flag 8 set)");
+  if (!c.gtaChi) TRY(dalloc(&c.gtaChi, (size_t)c.nz * c.G));
+  if (!c.gtaVec) {
+    TRY(dalloc(&c.gtaVec, 8 * (size_t)c.nc));
+    UMT_CUDA(cudaMemset(c.gtaVec, 0, 8 * (size_t)c.nc * 8));
+  }
+  if (!c.gtaSigS) TRY(dalloc(&c.gtaSigS, c.nz));
+  if (!c.gtaZ) TRY(dalloc(&c.gtaZ, 5 * (size_t)c.nz));
+  if (!c.red) TRY(dalloc(&c.red, 16));
+  return 0;
+}
+
+int umt103_gta_correction(const double *PhiPrev, double *correction, double *chi, int *grey_sweeps) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem");
+  if (!PhiPrev || !correction) return set_error(UMT_ERR_ARG, "null PhiPrev or correction");
+  TRY(gta_alloc(c));
+  const size_t ncG = (size_t)c.nc * c.G;
+  if (!c.PhiPrev) TRY(dalloc(&c.PhiPrev, ncG));
+  UMT_CUDA(cudaMemcpy(c.PhiPrev, PhiPrev, ncG * 8, cudaMemcpyHostToDevice));
+  int gs = 0;
+  TRY(gta_solve(c, c.gtaMaxKrylov, c.gtaTol, &gs, false));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  UMT_CUDA(cudaMemcpy(correction, c.gtaVec, (size_t)c.nc * 8, cudaMemcpyDeviceToHost));
+  if (chi) UMT_CUDA(cudaMemcpy(chi, c.gtaChi, (size_t)c.nz * c.G * 8, cudaMemcpyDeviceToHost));
+  if (grey_sweeps) *grey_sweeps = gs;
+  return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1190,15 +1234,7 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   const int prec = prm->precision;
   if (prec != UMT_FP64 && prec != UMT_FP32 && prec != UMT_MIXED) return set_error(UMT_ERR_ARG, "precision");
   if (prec == UMT_MIXED && prm->use_gta) return set_error(UMT_ERR_ARG, "UMT_MIXED does not combine with GTA");
-  if (prm->use_gta && !c.gta) return set_error(UMT_ERR_STATE, "GTA context not created (init flag 8 set)");
-  if (prm->use_gta) {
-    if (!c.gtaChi) TRY(dalloc(&c.gtaChi, (size_t)c.nz * c.G));
-    if (!c.gtaVec) {
-      TRY(dalloc(&c.gtaVec, 8 * (size_t)c.nc));
-      UMT_CUDA(cudaMemset(c.gtaVec, 0, 8 * (size_t)c.nc * 8));
-    }
-    if (!c.gtaSigS) TRY(dalloc(&c.gtaSigS, c.nz));
-  }
+  if (prm->use_gta) TRY(gta_alloc(c));
   int greySweeps = 0;
   const size_t ncG = (size_t)c.nc * c.G, nzG = (size_t)c.nz * c.G;
   if (!c.PhiPrev) TRY(dalloc(&c.PhiPrev, ncG));

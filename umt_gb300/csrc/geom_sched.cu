@@ -7,7 +7,12 @@
 // schedule did not produce.
 #include "umt_common.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace umt {
+
+#define TRY_RC(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
 
 // ---------------------------------------------------------------------------
 // Geometry: rt/geometryUCBxyz.F90:9-185 (area vectors of FP and EZ corner
@@ -202,7 +207,9 @@ int launch_projections(Ctx &c) {
 // the sum of Omega.A_fp over its corner faces decides the flow direction;
 // the downstream zone's need count is incremented and the upstream side's
 // face is marked as an exit.  A face whose corner faces disagree in sign
-// would need the reference's cycle list; it is reported as a cycle.
+// makes the upstream zone read some corners of the downstream zone before
+// they are computed: those corners go on the direction's cycle list (the
+// downstream zone is flagged in cycZ), as snneed.F90 does.
 // k_corner_order restates getDownStreamData (snac/getDownStreamData.F90:
 // 59-150): the corner solve order within a zone by repeated minloc of the
 // remaining EZ need; a zone whose corners cannot be ordered is "bad".
@@ -215,6 +222,7 @@ struct SchedArgs {
   uint8_t *exitMask, *bad;
   uint32_t *order;
   unsigned int *status;
+  uint8_t *cycZ;
 };
 
 __global__ void k_need(SchedArgs p) {
@@ -245,11 +253,11 @@ __global__ void k_need(SchedArgs p) {
           atomicAdd(&p.need[(size_t)a * p.nz + zone], 1);
           atomicOr((unsigned int *)(p.exitMask + (((size_t)a * p.nz + zOpp) & ~(size_t)3)),
                    (1u << fOpp) << (8 * (((size_t)a * p.nz + zOpp) & 3)));
-          if (nExit[face] > 0) atomicOr(p.status, UMT_DEV_CYCLE);
+          if (nExit[face] > 0) p.cycZ[i] = 1;
         } else if (afpm_Face[face] > 0.0) {
           atomicAdd(&p.need[(size_t)a * p.nz + zOpp], 1);
           atomicOr((unsigned int *)(p.exitMask + (i & ~(size_t)3)), (1u << face) << (8 * (i & 3)));
-          if (nInc[face] > 0) atomicOr(p.status, UMT_DEV_CYCLE);
+          if (nInc[face] > 0) p.cycZ[(size_t)a * p.nz + zOpp] = 1;
         }
       }
     }
@@ -285,10 +293,10 @@ __global__ void k_corner_order(SchedArgs p) {
       for (int m = 0; m < nDSC[c]; ++m) need[DSC[c][m]] -= 1;
       need[c] = 99;
     }
-    if (isbad) {
+    if (isbad) {                      // fixZone: the zone is swept from its corners' previous values
       ord = 0;
       for (int k = 0; k < nCorner; ++k) ord |= (uint32_t)k << (4 * k);
-      atomicOr(p.status, UMT_DEV_CYCLE);
+      p.cycZ[i] = 1;
     }
     p.order[i] = ord;
     p.bad[i] = isbad ? 1 : 0;
@@ -307,6 +315,13 @@ __global__ void k_seed(int nz, int A, const int *need, const uint8_t *bad, uint3
       level[i] = 0;
     }
   }
+}
+
+// zones with no upwind need, per direction
+__global__ void k_seed_count(int nz, int A, const int *need, int *count) {
+  const size_t n = (size_t)A * nz;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if (need[i] == 0) atomicAdd(&count[i / nz], 1);
 }
 
 // Stage h -> h+1 (the hyperplane loop of snac/snnext.F90:109-163): every item
@@ -354,46 +369,252 @@ __global__ void k_items2(size_t n, int nz, const uint32_t *items, const int *cOf
   }
 }
 
+// ---------------------------------------------------------------------------
+// Cycle breaking on the host, for the directions whose wavefront stalls.
+// Restates the decisions of snac/findseeds.F90:58-112 (no seed at all: the
+// boundary zone of least need starts, the zones across its non-exit faces go
+// on the cycle list) and snac/cyclebreaker.F90:88-143 with
+// snac/sccsearch.F90:8-187 (Tarjan's strongly connected components over the
+// zones not yet placed; in each component of more than one zone, the root's
+// incoming faces from zones still on the search stack are cut and those
+// zones' corners go on the cycle list; a root left with no need starts the
+// next stage).  The search visits zones in increasing order and faces in
+// face order, depth first, as the recursive reference does; it keeps an
+// explicit stack so that deep meshes cannot overflow the host stack.
+// ---------------------------------------------------------------------------
+struct DirGraph {
+  int nz;
+  const int *zoneFaces, *zoneOpp, *faceOpp;     // host copies [nz], [nz*UMT_MAXFACES]
+  int *need;                                    // [nz] this direction's slice
+  uint8_t *exitMask, *cyc;                      // [nz]
+  bool exit(int z, int f) const { return (exitMask[z] >> f) & 1u; }
+  void clear_exit(int z, int f) { exitMask[z] &= (uint8_t)~(1u << f); }
+};
+
+static int seed_fallback(DirGraph &g, std::vector<int> &freed) {
+  int minNeed = g.nz, zoneID = -1;
+  for (int z = 0; z < g.nz; ++z) {
+    bool bdy = false;
+    for (int f = 0; f < g.zoneFaces[z]; ++f) bdy |= g.zoneOpp[z * UMT_MAXFACES + f] < 0;
+    if (bdy && g.need[z] < minNeed) { zoneID = z; minNeed = g.need[z]; }
+  }
+  if (zoneID < 0) return -1;
+  g.need[zoneID] = 0;
+  for (int f = 0; f < g.zoneFaces[zoneID]; ++f) {
+    if (g.exit(zoneID, f)) continue;
+    const int zo = g.zoneOpp[zoneID * UMT_MAXFACES + f], fo = g.faceOpp[zoneID * UMT_MAXFACES + f];
+    if (zo >= 0) {
+      g.cyc[zo] = 1;
+      g.clear_exit(zo, fo);
+    }
+  }
+  freed.push_back(zoneID);
+  return 0;
+}
+
+static int break_cycles(DirGraph &g, std::vector<int> &freed) {
+  const int nz = g.nz;
+  std::vector<int> dfnum(nz, 0), lowlink(nz, 0), stk, breakList, tmp;
+  std::vector<char> isnew(nz, 0), onstack(nz, 0);
+  struct Frame { int zone, face; };
+  std::vector<Frame> frames;
+  for (int z = 0; z < nz; ++z) isnew[z] = g.need[z] != 0;
+  int ncount = 0;
+  auto enter = [&](int z) {
+    ++ncount;
+    dfnum[z] = lowlink[z] = ncount;
+    isnew[z] = 0;
+    stk.push_back(z);
+    onstack[z] = 1;
+    frames.push_back({z, 0});
+  };
+  auto finish = [&](int zone) {
+    if (lowlink[zone] != dfnum[zone]) return;
+    int z2 = stk.back();
+    stk.pop_back();
+    onstack[z2] = 0;
+    if (z2 == zone) return;
+    tmp.clear();
+    while (z2 != zone) {
+      tmp.push_back(z2);
+      z2 = stk.back();
+      stk.pop_back();
+    }
+    tmp.push_back(z2);
+    onstack[tmp[0]] = 1;
+    const int root = tmp.back();
+    for (int f = 0; f < g.zoneFaces[root]; ++f) {
+      const int zb = g.zoneOpp[root * UMT_MAXFACES + f], fb = g.faceOpp[root * UMT_MAXFACES + f];
+      if (zb >= 0 && onstack[zb] && g.exit(zb, fb)) {
+        g.cyc[zb] = 1;
+        g.need[root] -= 1;
+        g.clear_exit(zb, fb);
+        if (g.need[root] == 0) breakList.push_back(root);
+      }
+    }
+    for (int v : tmp) onstack[v] = 0;
+  };
+  for (int z0 = 0; z0 < nz; ++z0) {
+    if (!isnew[z0]) continue;
+    enter(z0);
+    while (!frames.empty()) {
+      Frame &fr = frames.back();
+      const int zone = fr.zone;
+      if (fr.face < g.zoneFaces[zone]) {
+        const int f = fr.face++;
+        if (!g.exit(zone, f)) continue;
+        const int z2 = g.zoneOpp[zone * UMT_MAXFACES + f];
+        if (z2 < 0) continue;
+        if (isnew[z2]) {
+          enter(z2);                              // invalidates fr
+        } else if (dfnum[z2] < dfnum[zone] && onstack[z2] && lowlink[z2] < lowlink[zone]) {
+          lowlink[zone] = lowlink[z2];
+        }
+      } else {
+        finish(zone);
+        frames.pop_back();
+        if (!frames.empty()) {
+          const int parent = frames.back().zone;
+          if (lowlink[zone] < lowlink[parent]) lowlink[parent] = lowlink[zone];
+        }
+      }
+    }
+  }
+  for (int z : breakList) {
+    if (g.need[z] == 0) freed.push_back(z);
+    else if (g.need[z] < 0) return -1;
+  }
+  return freed.empty() ? -1 : 0;
+}
+
+// Host copies of the mesh connectivity the breaker needs.
+struct HostConn {
+  std::vector<int> zoneFaces, zoneOpp, faceOpp, numCorner, cOffSet;
+};
+static int host_conn(Ctx &c, HostConn &h) {
+  h.zoneFaces.resize(c.nz); h.zoneOpp.resize((size_t)c.nz * UMT_MAXFACES); h.faceOpp.resize((size_t)c.nz * UMT_MAXFACES);
+  h.numCorner.resize(c.nz); h.cOffSet.resize(c.nz);
+  UMT_CUDA(cudaMemcpy(h.zoneFaces.data(), c.zoneFaces, c.nz * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(h.zoneOpp.data(), c.zoneOpp, h.zoneOpp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(h.faceOpp.data(), c.faceOpp, h.faceOpp.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(h.numCorner.data(), c.numCorner, c.nz * sizeof(int), cudaMemcpyDeviceToHost));
+  UMT_CUDA(cudaMemcpy(h.cOffSet.data(), c.cOffSet, c.nz * sizeof(int), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 int build_schedule(Ctx &c) {
   Schedule &s = c.sch;
   const size_t n = (size_t)c.A * c.nz;
   UMT_CUDA(cudaMemsetAsync(s.need, 0, n * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.exitMask, 0, ((n + 3) & ~(size_t)3), c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.cycZ, 0, n, c.stream));
+  UMT_CUDA(cudaMemsetAsync(s.level, 0xff, n * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.stageCount, 0, (c.nz + 2) * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.stageOffset, 0, (c.nz + 2) * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.nHyper, 0, c.A * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.processed, 0, sizeof(unsigned long long), c.stream));
   SchedArgs p{c.nz, c.nc, c.A, c.numCorner, c.cOffSet, c.zoneFaces, c.zoneOpp, c.faceOpp,
-              c.nCFaces, c.cEZ, c.CToFace, c.afp64, c.aez64, s.need, s.exitMask, s.bad, s.order, c.status};
+              c.nCFaces, c.cEZ, c.CToFace, c.afp64, c.aez64, s.need, s.exitMask, s.bad, s.order, c.status, s.cycZ};
   const int B = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
   k_need<<<B, 256, 0, c.stream>>>(p);
-  UMT_CUDA(cudaMemcpyAsync(s.needInit, s.need, n * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
   k_corner_order<<<B, 256, 0, c.stream>>>(p);
+  UMT_CUDA(cudaGetLastError());
+  HostConn hc;
+  bool haveConn = false;
+  s.breaks = 0;
+  // directions without a seed (findseeds.F90:71-112)
+  {
+    int *cnt = nullptr;
+    UMT_CUDA(cudaMalloc((void **)&cnt, c.A * sizeof(int)));
+    std::vector<int> hcnt(c.A);
+    cudaError_t e = cudaMemsetAsync(cnt, 0, c.A * sizeof(int), c.stream);
+    if (e == cudaSuccess) {
+      k_seed_count<<<B, 256, 0, c.stream>>>(c.nz, c.A, s.need, cnt);
+      e = cudaMemcpyAsync(hcnt.data(), cnt, c.A * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    cudaFree(cnt);
+    if (e != cudaSuccess) return set_error(-3, "seed count: %s", cudaGetErrorString(e));
+    for (int a = 0; a < c.A; ++a) {
+      if (hcnt[a] > 0) continue;
+      if (!haveConn) { TRY_RC(host_conn(c, hc)); haveConn = true; }
+      std::vector<int> need(c.nz);
+      std::vector<uint8_t> ex(c.nz), cy(c.nz);
+      const size_t o = (size_t)a * c.nz;
+      UMT_CUDA(cudaMemcpy(need.data(), s.need + o, c.nz * sizeof(int), cudaMemcpyDeviceToHost));
+      UMT_CUDA(cudaMemcpy(ex.data(), s.exitMask + o, c.nz, cudaMemcpyDeviceToHost));
+      UMT_CUDA(cudaMemcpy(cy.data(), s.cycZ + o, c.nz, cudaMemcpyDeviceToHost));
+      DirGraph g{c.nz, hc.zoneFaces.data(), hc.zoneOpp.data(), hc.faceOpp.data(), need.data(), ex.data(), cy.data()};
+      std::vector<int> freed;
+      if (seed_fallback(g, freed)) return set_error(-4, "direction %d has no zone to start from", a);
+      UMT_CUDA(cudaMemcpy(s.need + o, need.data(), c.nz * sizeof(int), cudaMemcpyHostToDevice));
+      UMT_CUDA(cudaMemcpy(s.exitMask + o, ex.data(), c.nz, cudaMemcpyHostToDevice));
+      UMT_CUDA(cudaMemcpy(s.cycZ + o, cy.data(), c.nz, cudaMemcpyHostToDevice));
+      ++s.breaks;
+    }
+  }
+  UMT_CUDA(cudaMemcpyAsync(s.needInit, s.need, n * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
   k_seed<<<B, 256, 0, c.stream>>>(c.nz, c.A, s.need, s.bad, s.items, s.stageCount, s.level, s.processed);
   UMT_CUDA(cudaGetLastError());
-  unsigned int st = 0;
-  UMT_CUDA(cudaMemcpyAsync(&st, c.status, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
-  UMT_CUDA(cudaStreamSynchronize(c.stream));
-  if (st & UMT_DEV_CYCLE)
-    return set_error(-4, "mesh has a zone face or zone corner cycle for some direction; "
-                         "lagged (cycle-list) sweeps are not supported by the device schedule");
-  // stages: launch in batches, stop when every item is placed
+  // stages: launch in batches; a stall with items left is a mesh cycle,
+  // broken on the host for every direction it holds up
   int h = 0;
   const int batch = 32;
   const int SB = 152 * 8;
   unsigned long long placed = 0;
-  int lastCount = -1;
   while (true) {
     for (int k = 0; k < batch && h < c.nz; ++k, ++h)
       k_stage<<<SB, 256, 0, c.stream>>>(h, c.nz, c.A, c.zoneFaces, c.zoneOpp, s.exitMask, s.bad, s.need,
                                         s.items, s.stageCount, s.stageOffset, s.level, s.nHyper, s.processed);
     UMT_CUDA(cudaGetLastError());
     UMT_CUDA(cudaMemcpyAsync(&placed, s.processed, sizeof(placed), cudaMemcpyDeviceToHost, c.stream));
-    UMT_CUDA(cudaMemcpyAsync(&lastCount, s.stageCount + h, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     UMT_CUDA(cudaStreamSynchronize(c.stream));
     if (placed == n) break;
-    if (lastCount == 0 || h >= c.nz)
-      return set_error(-4, "schedule stalled after %d stages (%llu of %zu items): mesh cycle", h, placed, n);
+    std::vector<int> cnt(h + 1), off(h + 1);
+    UMT_CUDA(cudaMemcpy(cnt.data(), s.stageCount, (h + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    UMT_CUDA(cudaMemcpy(off.data(), s.stageOffset, (h + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+    int h0 = -1;
+    for (int k = 1; k <= h; ++k)
+      if (cnt[k] == 0) { h0 = k; break; }
+    if (h0 < 0) {
+      if (h >= c.nz) return set_error(-4, "schedule: %llu of %zu items placed after %d stages", placed, n, h);
+      continue;                                   // still progressing
+    }
+    // stalled: stage h0 is empty and items remain
+    if (!haveConn) { TRY_RC(host_conn(c, hc)); haveConn = true; }
+    std::vector<int> need(n), lev(n);
+    std::vector<uint8_t> ex(n), cy(n), bad(n);
+    UMT_CUDA(cudaMemcpy(need.data(), s.need, n * sizeof(int), cudaMemcpyDeviceToHost));
+    UMT_CUDA(cudaMemcpy(lev.data(), s.level, n * sizeof(int), cudaMemcpyDeviceToHost));
+    UMT_CUDA(cudaMemcpy(ex.data(), s.exitMask, n, cudaMemcpyDeviceToHost));
+    UMT_CUDA(cudaMemcpy(cy.data(), s.cycZ, n, cudaMemcpyDeviceToHost));
+    UMT_CUDA(cudaMemcpy(bad.data(), s.bad, n, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> newItems;
+    for (int a = 0; a < c.A; ++a) {
+      const size_t o = (size_t)a * c.nz;
+      bool left = false;
+      for (int z = 0; z < c.nz && !left; ++z) left = lev[o + z] < 0;
+      if (!left) continue;
+      DirGraph g{c.nz, hc.zoneFaces.data(), hc.zoneOpp.data(), hc.faceOpp.data(), need.data() + o, ex.data() + o,
+                 cy.data() + o};
+      std::vector<int> freed;
+      if (break_cycles(g, freed))
+        return set_error(-4, "direction %d: a dependency cycle could not be broken", a);
+      for (int z : freed) {
+        newItems.push_back((uint32_t)(o + z) | (bad[o + z] ? 0x80000000u : 0u));
+        lev[o + z] = h0;
+      }
+    }
+    if (newItems.empty()) return set_error(-4, "schedule stalled with no cycle to break");
+    ++s.breaks;
+    const int nn = (int)newItems.size();
+    UMT_CUDA(cudaMemcpy(s.need, need.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(s.level, lev.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(s.exitMask, ex.data(), n, cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(s.cycZ, cy.data(), n, cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(s.items + off[h0], newItems.data(), nn * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    UMT_CUDA(cudaMemcpy(s.stageCount + h0, &nn, sizeof(int), cudaMemcpyHostToDevice));
+    h = h0;                                       // the wavefront resumes from the freed zones
   }
   {
     const int B2 = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
@@ -411,6 +632,85 @@ int build_schedule(Ctx &c) {
     s.nStages = k + 1;
     s.maxStageItems = std::max(s.maxStageItems, s.hCount[k]);
   }
+  // the cycle list of every direction: the corners of its flagged zones
+  {
+    std::vector<uint8_t> cy(n);
+    UMT_CUDA(cudaMemcpy(cy.data(), s.cycZ, n, cudaMemcpyDeviceToHost));
+    if (!haveConn) { TRY_RC(host_conn(c, hc)); haveConn = true; }
+    std::vector<long long> rows;
+    s.hCycOff.assign(c.A + 1, 0);
+    for (int a = 0; a < c.A; ++a) {
+      s.hCycOff[a] = (long long)rows.size();
+      for (int z = 0; z < c.nz; ++z)
+        if (cy[(size_t)a * c.nz + z])
+          for (int k = 0; k < hc.numCorner[z]; ++k) rows.push_back((long long)a * c.nc + hc.cOffSet[z] + k);
+    }
+    s.hCycOff[c.A] = (long long)rows.size();
+    s.nCyc = (long long)rows.size();
+    if (s.cycRow) { cudaFree(s.cycRow); s.cycRow = nullptr; }
+    if (s.nCyc) {
+      UMT_CUDA(cudaMalloc((void **)&s.cycRow, s.nCyc * sizeof(long long)));
+      UMT_CUDA(cudaMemcpy(s.cycRow, rows.data(), s.nCyc * sizeof(long long), cudaMemcpyHostToDevice));
+    }
+  }
+  return 0;
+}
+
+// psi_new rows of the cycle list <- the stored previous values (initFromCycleList,
+// control/constructDynMemory.F90:111-161), before a sweep's first stage
+template <typename T>
+__global__ void k_cycle_init(long long nCyc, int G, const long long *row, const T *store, T *psi) {
+  const long long m = nCyc * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i / G;
+    psi[row[k] * G + (i - k * G)] = store[i];
+  }
+}
+
+// the stored values <- psi_new rows (updateCycleList, :166-214), after the last stage
+template <typename T>
+__global__ void k_cycle_update(long long nCyc, int G, const long long *row, T *store, const T *psi) {
+  const long long m = nCyc * G;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i / G;
+    store[i] = psi[row[k] * G + (i - k * G)];
+  }
+}
+
+int enqueue_cycle_init(Ctx &c, int precision, int cur) {
+  const Schedule &s = c.sch;
+  if (!s.nCyc) return 0;
+  const int blocks = (int)std::min<long long>((s.nCyc * c.G + 255) / 256, 152 * 8);
+  if (precision == 0) k_cycle_init<double><<<blocks, 256, 0, c.stream>>>(s.nCyc, c.G, s.cycRow, c.cycPsi64, c.psi64[1 - cur]);
+  else k_cycle_init<float><<<blocks, 256, 0, c.stream>>>(s.nCyc, c.G, s.cycRow, c.cycPsi32, c.psi32[1 - cur]);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int enqueue_cycle_update(Ctx &c, int precision, int cur) {
+  const Schedule &s = c.sch;
+  if (!s.nCyc) return 0;
+  const int blocks = (int)std::min<long long>((s.nCyc * c.G + 255) / 256, 152 * 8);
+  if (precision == 0) k_cycle_update<double><<<blocks, 256, 0, c.stream>>>(s.nCyc, c.G, s.cycRow, c.cycPsi64, c.psi64[1 - cur]);
+  else k_cycle_update<float><<<blocks, 256, 0, c.stream>>>(s.nCyc, c.G, s.cycRow, c.cycPsi32, c.psi32[1 - cur]);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// The stored cycle values <- the saved angular flux (Psi) at those corners,
+// as the reference sets cyclePsi at the start of a cycle
+// (control/initializeRadiationField_OMPOL.F90:105); allocates the stores.
+int cycle_from_psi(Ctx &c) {
+  const Schedule &s = c.sch;
+  if (!s.nCyc) return 0;
+  const size_t m = (size_t)s.nCyc * c.G;
+  if (c.psi64[0] && !c.cycPsi64) UMT_CUDA(cudaMalloc((void **)&c.cycPsi64, m * sizeof(double)));
+  if (c.psi32[0] && !c.cycPsi32) UMT_CUDA(cudaMalloc((void **)&c.cycPsi32, m * sizeof(float)));
+  const int blocks = (int)std::min<long long>((s.nCyc * c.G + 255) / 256, 152 * 8);
+  if (c.cycPsi64) k_cycle_update<double><<<blocks, 256, 0, c.stream>>>(s.nCyc, c.G, s.cycRow, c.cycPsi64, c.psi64[c.cur64]);
+  if (c.cycPsi32) k_cycle_update<float><<<blocks, 256, 0, c.stream>>>(s.nCyc, c.G, s.cycRow, c.cycPsi32, c.psi32[c.cur32]);
+  UMT_CUDA(cudaGetLastError());
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
   return 0;
 }
 

@@ -638,7 +638,9 @@ int umt103_init_rz(const UmtMeshRZ *m, const UmtQuadRZ *q, int ngr, int flags) {
   int rc = init_context(c, &m3, &q3, ngr, precFlags);
   if (rc) { delete r; return rc; }
   c.rz = r;
-  // the schedule must be cycle-free (convex RZ zones have no intra-zone cycles)
+  // the schedule must be cycle-free (convex RZ zones have no intra-zone
+  // cycles; the RZ sweep carries no cycle list)
+  if (c.sch.nCyc > 0) return set_error(UMT_ERR_CYCLE, "RZ: the mesh has a dependency cycle, not supported");
   {
     std::vector<uint8_t> bad((size_t)A * nz);
     UMT_CUDA(cudaMemcpy(bad.data(), c.sch.bad, bad.size(), cudaMemcpyDeviceToHost));

@@ -10,6 +10,9 @@
 // reductions accumulate in FP64.
 #include "umt_common.cuh"
 
+#include <algorithm>
+#include <cmath>
+
 namespace umt {
 
 constexpr double WTISO = 0.079577471545947667884;   // 1/(4 pi), mods/Size_mod.F90:281
@@ -281,28 +284,151 @@ __global__ void k_gta_correct(int nc, int G, const int *cToZone, const double *c
   }
 }
 
+// Stretched-TSA opacities of each zone (rt/setGTAOpacity.F90:225-232):
+// eps = 1/sqrt(1 - sigma_s/sigma_t) of the grey problem and the stretched
+// total opacity sigma_t/eps, for which the stretched problem's scattering
+// term vanishes.  sigt1 keeps sigma_t for the restore after a stretched sweep.
+__global__ void k_gta_stretch(int nz, const double *greySigt, const double *greySigs, double *eps, double *sigt1,
+                              double *sigt2) {
+  for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const double gt = greySigt[z];
+    const double e = 1.0 / sqrt(1.0 - greySigs[z] / gt);
+    eps[z] = e;
+    sigt1[z] = gt;
+    sigt2[z] = gt / e;
+  }
+}
+
+// Stretched-TSA sweep source (snac/GTASweep.F90, GTA%ID = 2):
+// STotal = wtiso sigma_s eps (P - Pold)
+__global__ void k_gta_source2(int nc, const int *cToZone, const double *greySigs, const double *eps, const double *P,
+                              const double *Pold, double *STotal) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int z = cToZone[c];
+    STotal[c] = WTISO * greySigs[z] * eps[z] * (P[c] - (Pold ? Pold[c] : 0.0));
+  }
+}
+
+// Zone radiation energy density sum_c V_c sum_g phi_c,g / V_z (rt/GTASolver.F90
+// ZoneLoop) and pzOld = 0.
+__global__ void k_gta_zone_energy(int nz, int G, const int *numCorner, const int *cOffSet, const double *Volume,
+                                  const double *VolumeZone, const double *Phi, double *radE, double *pzOld) {
+  for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const int c0 = cOffSet[z], nC = numCorner[z];
+    double e = 0.0;
+    for (int k = 0; k < nC; ++k) {
+      double s = 0.0;
+      for (int g = 0; g < G; ++g) s += Phi[(size_t)(c0 + k) * G + g];
+      e += Volume[c0 + k] * s;
+    }
+    radE[z] = e / VolumeZone[z];
+    pzOld[z] = 0.0;
+  }
+}
+
+// Convergence of the zone-averaged grey correction (rt/GTASolver.F90
+// CorrectionZoneLoop): out[0] += V_z (pz - pzOld)^2, out[1] += V_z (radE +
+// pz)^2, out[2] = max |pz - pzOld| / |radE + pz| (bit pattern of a
+// non-negative double, so an integer max orders it); pzOld = pz.
+__global__ void k_gta_converge(int nz, const int *numCorner, const int *cOffSet, const double *Volume,
+                               const double *VolumeZone, const double *x, const double *radE, double *pzOld,
+                               double *out) {
+  double v[2] = {0.0, 0.0};
+  double mx = 0.0;
+  for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const int c0 = cOffSet[z], nC = numCorner[z];
+    double pz = 0.0;
+    for (int k = 0; k < nC; ++k) pz += Volume[c0 + k] * x[c0 + k];
+    pz /= VolumeZone[z];
+    const double err = pz - pzOld[z];
+    const double phiNew = radE[z] + pz;
+    v[0] += VolumeZone[z] * err * err;
+    v[1] += VolumeZone[z] * phiNew * phiNew;
+    if (phiNew != 0.0) mx = fmax(mx, fabs(err / phiNew));
+    pzOld[z] = pz;
+  }
+  block_reduce_add<2>(v, out);
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long *>(out + 2), (unsigned long long)__double_as_longlong(mx));
+}
+
+// Inner products weighted by sigma_s,grey V (rt/scat_prod.F90, scat_prod1.F90):
+// out[0] += sum x y s, out[1] += sum u w s with s = sigma_s,grey(zone) V_c;
+// a null y or w stands for 1 (scat_prod1), a null u skips the second sum.
+__global__ void k_sdot2(int nc, const int *cToZone, const double *greySigs, const double *Volume, const double *x,
+                        const double *y, const double *u, const double *w, double *out2) {
+  double v[2] = {0.0, 0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const double s = greySigs[cToZone[c]] * Volume[c];
+    v[0] += x[c] * (y ? y[c] : 1.0) * s;
+    if (u) v[1] += u[c] * (w ? w[c] : 1.0) * s;
+  }
+  block_reduce_add<2>(v, out2);
+}
+
+// Grey problem of this iterate: spectrum and grey opacities (k_gta_spectrum),
+// the stretched-TSA opacities, the grey source R = sum_g sigma_s,g (phi_g -
+// phi_g_prev) in slot 7 of the vectors, the zone radiation energy.
 int gta_prepare(Ctx &c) {
   Ctx &q = *c.gta;
   const int B = 152 * 4;
+  double *Z = c.gtaZ;                              // [5][nz]: eps, sigt1, sigt2, radE, pzOld
   k_gta_spectrum<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, c.G, c.tau, c.gtaSpectrum, c.numCorner, c.cOffSet, c.Volume,
                                                           c.Sigt, c.SigS, c.Phi, c.PhiPrev, c.gtaChi, q.Sigt,
                                                           c.gtaSigS);
+  k_gta_stretch<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, q.Sigt, c.gtaSigS, Z, Z + c.nz, Z + 2 * (size_t)c.nz);
   UMT_CUDA(cudaMemcpyAsync(q.SigS, c.gtaSigS, c.nz * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
-  // R lives in slot 7 of the BiCGStab vectors
   k_gta_residual<<<B, 256, 0, c.stream>>>(c.nc, c.G, c.cToZone, c.SigS, c.Phi, c.PhiPrev, c.gtaVec + 7 * (size_t)c.nc);
+  k_gta_zone_energy<<<(c.nz + 127) / 128, 128, 0, c.stream>>>(c.nz, c.G, c.numCorner, c.cOffSet, c.Volume,
+                                                              c.VolumeZone, c.Phi, Z + 3 * (size_t)c.nz,
+                                                              Z + 4 * (size_t)c.nz);
   UMT_CUDA(cudaGetLastError());
   return 0;
 }
 
-// y <- K x + wR * K0 R  (one grey sweep; result is the grey context's Phi)
-int gta_apply(Ctx &c, const double *x, double wR) {
+// out = M P: the grey operator of rt/GreySweep.F90 (GreySweep): one grey S2
+// sweep of wtiso (sigma_s P + [R]) with sigma_t, then the stretched-TSA sweep
+// of wtiso sigma_s eps (P1 - P) with sigma_t/eps, added to it.  P may be null
+// (zero); out must not alias P.  Two grey sweeps.
+int gta_op(Ctx &c, const double *P, double *out, bool withSource) {
   Ctx &q = *c.gta;
-  k_gta_source<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.cToZone, c.gtaSigS, x, c.gtaVec + 7 * (size_t)c.nc, wR,
-                                              q.STotal);
+  double *Z = c.gtaZ;
+  const size_t n = (size_t)c.nc;
+  k_gta_source<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.cToZone, c.gtaSigS, P, c.gtaVec + 7 * n,
+                                              withSource ? 1.0 : 0.0, q.STotal);
   UMT_CUDA(cudaGetLastError());
   UMT_CUDA(cudaStreamSynchronize(c.stream));
   TRY_SI(launch_sweep_once(q, 0, true));
+  UMT_CUDA(cudaMemcpyAsync(out, q.Phi, n * 8, cudaMemcpyDeviceToDevice, q.stream));
+  k_gta_source2<<<152 * 4, 256, 0, q.stream>>>(c.nc, c.cToZone, c.gtaSigS, Z, out, P, q.STotal);
+  UMT_CUDA(cudaMemcpyAsync(q.Sigt, Z + 2 * (size_t)c.nz, c.nz * 8, cudaMemcpyDeviceToDevice, q.stream));
+  TRY_SI(launch_sweep_once(q, 0, true));
+  UMT_CUDA(cudaMemcpyAsync(q.Sigt, Z + c.nz, c.nz * 8, cudaMemcpyDeviceToDevice, q.stream));
+  k_axpbypcz<<<152 * 4, 256, 0, q.stream>>>(c.nc, 1.0, q.Phi, 1.0, out, 0.0, nullptr);
+  UMT_CUDA(cudaGetLastError());
   UMT_CUDA(cudaStreamSynchronize(q.stream));
+  return 0;
+}
+
+int gta_sdot2(Ctx &c, const double *x, const double *y, const double *u, const double *w, double *h2) {
+  UMT_CUDA(cudaMemsetAsync(c.red + 4, 0, 2 * sizeof(double), c.stream));
+  k_sdot2<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.cToZone, c.gtaSigS, c.Volume, x, y, u, w, c.red + 4);
+  UMT_CUDA(cudaMemcpyAsync(h2, c.red + 4, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+// relative change of the zone-averaged correction: max(pointwise, L2)
+int gta_converge(Ctx &c, const double *x, double *rel) {
+  double *Z = c.gtaZ;
+  UMT_CUDA(cudaMemsetAsync(c.red + 10, 0, 3 * sizeof(double), c.stream));
+  k_gta_converge<<<(c.nz + 255) / 256, 256, 0, c.stream>>>(c.nz, c.numCorner, c.cOffSet, c.Volume, c.VolumeZone, x,
+                                                           Z + 3 * (size_t)c.nz, Z + 4 * (size_t)c.nz, c.red + 10);
+  double h[3];
+  UMT_CUDA(cudaMemcpyAsync(h, c.red + 10, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  const double l2 = h[1] != 0.0 ? std::sqrt(std::fabs(h[0] / h[1])) : 0.0;
+  *rel = std::max(h[2], l2);
   return 0;
 }
 

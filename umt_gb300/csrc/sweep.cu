@@ -335,7 +335,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
     c.sweepGT[prec] = GT;
   }
   const int TEAMS = SWEEP_NT / GT;
-  c.launchesPerSweep[prec] = c.sch.nStages + 1 + (sizeof(T) == 4 ? 2 : 0);
+  c.launchesPerSweep[prec] = c.sch.nStages + 1 + (sizeof(T) == 4 ? 2 : 0) + (c.sch.nCyc ? 2 : 0);
   bool done = false;
   if constexpr (sizeof(T) == 4) {
     c.exitsThrough = false;                   // set again by the zone-program path below
@@ -344,6 +344,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
     const size_t m = (size_t)c.nc * c.G;
     k_to_float<<<(int)std::min<size_t>((m + 255) / 256, 4096), 256, 0, c.stream>>>(m, c.STotal, c.STotal32);
     if (c.tileGT == 0) default_tile(c.G, &c.tileGT, &c.tileGPL);
+    TRY_RC(enqueue_cycle_init(c, prec, cur));
     if (c.tileGT > 0 && sweep32_supported(c.G, c.tileGT, c.tileGPL)) {
       if (!c.rec32Ready) {
         int rc = prepare_sweep32(c);
@@ -355,6 +356,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
       done = true;
     }
   }
+  if constexpr (sizeof(T) == 8) TRY_RC(enqueue_cycle_init(c, prec, cur));
   for (int s = 0; s < c.sch.nStages && !done; ++s) {
     const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;
     switch (GT) {
@@ -366,6 +368,7 @@ static int enqueue_sweep(Ctx &c, int cur) {
       default: k_sweep<T, 32><<<blocks, SWEEP_NT, 0, c.stream>>>(p, s); break;
     }
   }
+  TRY_RC(enqueue_cycle_update(c, prec, cur));
   if (!c.inSIGraph) TRY_RC(record_mid(c));       // no event nodes inside a conditional body
   const size_t ncG = (size_t)c.nc * c.G;
   const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);

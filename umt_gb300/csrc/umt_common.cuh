@@ -39,6 +39,13 @@ struct Schedule {
   int nStages = 0;
   std::vector<int> hCount, hOffset;         // host copies
   int maxStageItems = 0;
+  uint8_t *cycZ = nullptr;        // [A*nz] 1: the zone's corners are on the direction's cycle list
+  // cycle list (constructDynMemory.F90:56-214): corner rows of psi read
+  // before this sweep computes them, taken from the previous sweep
+  long long *cycRow = nullptr;    // [nCyc] a*nc + c
+  long long nCyc = 0;
+  std::vector<long long> hCycOff; // [A+1] per-direction offsets into cycRow
+  int breaks = 0;                 // cycle-breaker passes the build needed
 };
 
 struct Ctx {
@@ -106,6 +113,8 @@ struct Ctx {
   float *psiB32h = nullptr;                     // boundary rows of those sweeps (incoming rows stay zero)
   cudaGraphExec_t graphsH[2] = {nullptr, nullptr};
   double *mixX = nullptr, *mixR = nullptr, *mixD = nullptr;   // [nc][G] outer iterate, residual, correction
+  double *cycPsi64 = nullptr;                   // [nCyc][G] previous-sweep flux of the cycle-list corners
+  float *cycPsi32 = nullptr;
   double *red = nullptr;                        // [8] reduction slots
   // angular flux, double buffered: psi[cur] = saved Psi, psi[1-cur] = new
   double *psi64[2] = {nullptr, nullptr};
@@ -145,6 +154,7 @@ struct Ctx {
   double *gtaChi = nullptr;                     // [nz][G] correction spectrum
   double *gtaVec = nullptr;                     // [8][nc] BiCGStab vectors
   double *gtaSigS = nullptr;                    // [nz] grey scattering (for inner products)
+  double *gtaZ = nullptr;                       // [5][nz] stretched-TSA eps, sigma_t, sigma_t/eps; zone energy; last zone correction
   int gtaMaxKrylov = 10;                        // BiCGStab iterations per correction (2 grey sweeps each)
   double gtaTol = 1.0e-4;                       // BiCGStab relative residual
   int gtaSpectrum = 0;                          // correction spectrum (see k_gta_spectrum)
@@ -168,6 +178,11 @@ int set_error(int code, const char *fmt, ...);
 int launch_geometry(Ctx &c);
 int launch_projections(Ctx &c);
 int build_schedule(Ctx &c);
+// cycle list: psi_new rows <- stored previous values before a sweep, and the
+// stored values <- psi_new rows after it (geom_sched.cu)
+int enqueue_cycle_init(Ctx &c, int precision, int cur);
+int enqueue_cycle_update(Ctx &c, int precision, int cur);
+int cycle_from_psi(Ctx &c);
 // launchers (sweep TU)
 int capture_sweep_graph(Ctx &c, int precision, cudaGraph_t *out);
 int launch_sweep_once(Ctx &c, int precision, bool tally);
@@ -192,7 +207,9 @@ int launch_residual(Ctx &c, const double *X, double *R, double *out2);
 int launch_inner_update(Ctx &c, const double *R, double *D, double *delta, double *deltaPrev, double *out3);
 // grey transport acceleration (si.cu)
 int gta_prepare(Ctx &c);
-int gta_apply(Ctx &c, const double *x, double wR);
+int gta_op(Ctx &c, const double *P, double *out, bool withSource);
+int gta_sdot2(Ctx &c, const double *x, const double *y, const double *u, const double *w, double *h2);
+int gta_converge(Ctx &c, const double *x, double *rel);
 int gta_axpbypcz(Ctx &c, int n, double a, const double *x, double b, double *y, double cc, const double *z);
 int gta_dot2(Ctx &c, int n, const double *x, const double *y, const double *u, const double *w, double *h2);
 int gta_correct(Ctx &c, const double *eps);

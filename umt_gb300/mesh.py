@@ -141,12 +141,19 @@ class Mesh:
         return self.cToZone
 
 
-def build_tiled_mesh(nx: int, ny: int, nz: int) -> Mesh:
+def build_tiled_mesh(nx: int, ny: int, nz: int, perturb: float = 0.0, seed: int = 0) -> Mesh:
     """Unit-cube mesh of nx x ny x nz tiles, one zone layer per tile.
 
     Zones are numbered tile by tile (x fastest, then y, then z) and by the
     fixed polygon order inside a tile, which keeps neighbours close in memory
     (the role of the reference's k-d tree zone reordering).
+
+    perturb > 0 moves every interior lattice vertex by a seeded random
+    displacement of up to `perturb` lattice spacings along each axis
+    (boundary vertices stay on their boundary planes).  The faces then stop
+    being planar, and for some directions a zone face is partly incoming and
+    partly outgoing, a zone's corners cannot be ordered, or zones depend on
+    one another in a loop: the mesh cycles that Teton's cycle list handles.
     """
     U = TILE_UNITS
     LX, LY = U * nx + 1, U * ny + 1
@@ -194,6 +201,17 @@ def build_tiled_mesh(nx: int, ny: int, nz: int) -> Mesh:
     gz = (tk[:, None] + c_lz[None, :]).ravel()
     vid = (gz * LY + gy) * LX + gx                                  # [ncornr]
     px = np.stack([gx / (U * nx), gy / (U * ny), gz / float(nz)], axis=1)
+    if perturb > 0.0:
+        LZ = nz + 1
+        rng = np.random.Generator(np.random.Philox(seed))
+        d = rng.uniform(-perturb, perturb, size=(LZ * LY * LX, 3))
+        lx = np.arange(LZ * LY * LX) % LX
+        ly = (np.arange(LZ * LY * LX) // LX) % LY
+        lz = np.arange(LZ * LY * LX) // (LX * LY)
+        d[(lx == 0) | (lx == LX - 1), 0] = 0.0
+        d[(ly == 0) | (ly == LY - 1), 1] = 0.0
+        d[(lz == 0) | (lz == LZ - 1), 2] = 0.0
+        px = px + d[vid] * np.array([1.0 / (U * nx), 1.0 / (U * ny), 1.0 / nz])
 
     # ---- per-corner template connectivity ------------------------------------
     ncf_t = np.concatenate([t["ncf"] for t in tmpl])
