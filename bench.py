@@ -267,6 +267,78 @@ def time_to_converge(lib, prob, use_gta=False, tol64=1e-8, tol32=1e-7):
             "tolerance_fp64": tol64, "tolerance_fp32": tol32}
 
 
+def run_shard(args, world, rank, local):
+    """--shard: one source-iteration step of the config-2 problem with its
+    directions split over the ranks (one GPU each): every rank builds the
+    scattering source on its device and sweeps its block of directions
+    (umt103_si_step), the device PhiTotal is summed over ranks in place by an
+    NCCL all-reduce (a torch view of umt103_phi_device), and the change norm
+    is taken on the device.  The problem's total work is fixed (strong
+    scaling); value = units of the whole problem / max step time over ranks."""
+    import torch
+    from umt_gb300 import build, capi, sharding
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build.build()
+    lib = capi.Library()
+    lib.select_device(local)
+    prec = capi.UMT_FP32 if args.precision == "fp32" else capi.UMT_FP64
+    prob = make_problem(args.tiles, args.config)
+    m = prob.mesh
+    A, G = len(prob.weight), prob.ngr
+    dirs = sharding.direction_shards(A, world)[rank]
+    sw = sharding.DeviceSweeper(lib, prob, dirs, prec)
+    phi = sw.phi_tensor()
+    reduce = sharding.torch_allreduce_inplace() if dist else (lambda t: t)
+    phi.zero_()
+    torch.cuda.synchronize()
+    sw.change()
+
+    def step():
+        sw.step()
+        reduce(phi)
+        torch.cuda.synchronize()
+        return sw.change()
+
+    for _ in range(args.warmup):
+        step()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            rel = step()
+            times.append(time.perf_counter() - t0)
+    t = sum(times) / len(times)
+    if dist:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+        dist.barrier()
+    units = m.ncornr * A * G
+    if rank == 0:
+        line = {"metric": METRIC + " (angle-sharded source iteration step)", "value": t * 1e9 / units, "unit": "ns",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+                "higher_is_better": False, "scaling": "strong", "vs_baseline": None,
+                "dtype": "f32" if prec == capi.UMT_FP32 else "f64", "data": "synthetic",
+                "config": {"workload": f"multigroup scattering, {args.tiles}^3 tiles, {A} directions, {G} groups",
+                           "materials": MATERIALS[args.config],
+                           "directions_per_rank": [len(d) for d in sharding.direction_shards(A, world)],
+                           "parallelism": f"angle{world}",
+                           "collective": "NCCL all-reduce of PhiTotal in place (%d FP64 values) per step" % (m.ncornr * G),
+                           "l2": "inputs larger than L2"},
+                "last_rel_change": rel, "timing": "host wall time of each step (it ends with a device sync)",
+                "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def ttc_learned(args, lib):
     """Time to converge on the strongly scattering distribution (config 5:
     sigma_t log-uniform on [1, 1e3], c in [0.95, 0.999], 32 groups, 128
@@ -404,87 +476,109 @@ def config4_device_bytes(t, P, G):
 
 def run_config4(args):
     """Config 4: independent problems of uneven size resident in separate
-    contexts, swept from one graph launch (umt103_batch_sweep), against the
-    same contexts swept one after another.  The 64 draws hold about 430 GB in
-    FP32, more than one GPU, so the draws are taken in order while their
-    estimated device memory stays within --c4-budget GB; each problem's host
-    arrays are freed once its context holds them."""
+    contexts, swept from one graph launch per batch (umt103_batch_sweep),
+    against the same contexts swept one after another.  The 64 draws hold
+    about 430 GB in FP32, more than one GPU, so they are taken in order in
+    sub-batches whose estimated device memory stays within --c4-budget GB;
+    each sub-batch is one graph launch, timed, then released before the
+    next is built.  The group tile of each problem shape is tuned once
+    (umt103_autotune_contexts) and applied in the batch.  Reported: the
+    aggregate over all draws (sum of units / sum of sub-batch times)."""
     import gc
     from umt_gb300 import build, capi
     from umt_gb300.problems import synthetic_problem
     build.build()
     lib = capi.Library()
     draws = config4_draws(tiles=tuple(args.c4_tiles))
-    taken, used = [], 0.0
+    batches, cur, used = [], [], 0.0
     for d in draws:
         est = config4_device_bytes(*d[:3])
-        if used + est > args.c4_budget * 1e9:
-            break
-        taken.append(d); used += est
-    ids, units, balg_units = [], 0, 0.0
-    for (t, P, G, seed) in taken:
-        pr = synthetic_problem((t,) * 3, P, P, G, seed=seed, time_dependent=True)
-        cid = lib.context_create()
-        lib.context_select(cid)
-        lib.init(pr.mesh, pr.omega, pr.weight, G, flags=2 | 8)
-        lib.set_materials(pr.sigt, pr.sigs, pr.tau)
-        lib.set_psi(pr.psi0, None)
-        lib.set_source(np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi))
-        u = pr.mesh.ncornr * len(pr.weight) * G
-        units += u
-        balg_units += b_alg(G, len(pr.weight), 4, 4) * u
-        ids.append(cid)
-        del pr
-        gc.collect()
-    lib.context_select(0)
-    for _ in range(args.warmup):
-        lib.batch_sweep(ids, capi.UMT_FP32)
-    for cid in ids:
-        lib.context_select(cid)
-        for _ in range(args.warmup):
-            lib.sweep_resident(False, capi.UMT_FP32)
-    lib.context_select(0)
+        if cur and used + est > args.c4_budget * 1e9:
+            batches.append(cur)
+            cur, used = [], 0.0
+        cur.append(d)
+        used += est
+    if cur:
+        batches.append(cur)
+    if args.c4_max_batches:
+        batches = batches[:args.c4_max_batches]
+    tot_units, tot_balg = 0, 0.0
+    tb_ms = ts_ms = wb_ms = ws_ms = 0.0
+    per_batch = []
     with ClockSampler(0) as clk:
-        batch_ms, batch_wall = [], []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            batch_ms.append(lib.batch_sweep(ids, capi.UMT_FP32))
-            batch_wall.append((time.perf_counter() - t0) * 1e3)
-        seq_ms, seq_wall = [], []
-        for _ in range(args.steps):
-            tot = 0.0
-            t0 = time.perf_counter()
+        for taken in batches:
+            ids, units, balg_units = [], 0, 0.0
+            for (t, P, G, seed) in taken:
+                pr = synthetic_problem((t,) * 3, P, P, G, seed=seed, time_dependent=True)
+                cid = lib.context_create()
+                lib.context_select(cid)
+                lib.init(pr.mesh, pr.omega, pr.weight, G, flags=2 | 8)
+                lib.set_materials(pr.sigt, pr.sigs, pr.tau)
+                lib.set_psi(pr.psi0, None)
+                lib.set_source(np.repeat(pr.q_ext, pr.mesh.numCorner, axis=0) / (4 * np.pi))
+                u = pr.mesh.ncornr * len(pr.weight) * G
+                units += u
+                balg_units += b_alg(G, len(pr.weight), 4, 4) * u
+                ids.append(cid)
+                del pr
+                gc.collect()
+            lib.context_select(0)
+            if not args.c4_no_tune:
+                lib.autotune_contexts(ids, reps=1)
+            for _ in range(args.warmup):
+                lib.batch_sweep(ids, capi.UMT_FP32)
             for cid in ids:
                 lib.context_select(cid)
-                lib.sweep_resident(False, capi.UMT_FP32)
-                tot += lib.timing()[0]
-            seq_wall.append((time.perf_counter() - t0) * 1e3)
-            seq_ms.append(tot)
-    lib.context_select(0)
-    for cid in ids:
-        lib.context_destroy(cid)
-    t_b = statistics.median(batch_ms)
-    t_s = statistics.median(seq_ms)
-    w_b, w_s = statistics.median(batch_wall), statistics.median(seq_wall)
+                for _ in range(args.warmup):
+                    lib.sweep_resident(False, capi.UMT_FP32)
+            lib.context_select(0)
+            batch_ms, batch_wall = [], []
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                batch_ms.append(lib.batch_sweep(ids, capi.UMT_FP32))
+                batch_wall.append((time.perf_counter() - t0) * 1e3)
+            seq_ms, seq_wall = [], []
+            for _ in range(args.steps):
+                tot = 0.0
+                t0 = time.perf_counter()
+                for cid in ids:
+                    lib.context_select(cid)
+                    lib.sweep_resident(False, capi.UMT_FP32)
+                    tot += lib.timing()[0]
+                seq_wall.append((time.perf_counter() - t0) * 1e3)
+                seq_ms.append(tot)
+            lib.context_select(0)
+            for cid in ids:
+                lib.context_destroy(cid)
+            b, sq = statistics.median(batch_ms), statistics.median(seq_ms)
+            wb, ws = statistics.median(batch_wall), statistics.median(seq_wall)
+            tb_ms += b; ts_ms += sq; wb_ms += wb; ws_ms += ws
+            tot_units += units
+            tot_balg += balg_units
+            per_batch.append({"problems": len(taken), "units": units, "batch_ms": b, "sequential_ms": sq,
+                              "batch_wall_ms": wb, "sequential_wall_ms": ws,
+                              "draws": [list(d[:3]) for d in taken]})
     peak, src = peaks()
-    achieved = balg_units / (t_b * 1e-3) / 1e9
-    line = {"metric": METRIC, "value": t_b * 1e6 / units, "unit": "ns", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_b, "higher_is_better": False, "scaling": "weak",
+    achieved = tot_balg / (tb_ms * 1e-3) / 1e9
+    ndraws = sum(len(t) for t in batches)
+    line = {"metric": METRIC, "value": tb_ms * 1e6 / tot_units, "unit": "ns", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tb_ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch of independent problems (tiles per axis U{%d..%d}, G in {4..64}, "
-                                   "32 or 128 directions; seed 4), one graph launch" % tuple(args.c4_tiles),
-                       "problems": len(taken), "of_draws": len(draws), "device_budget_gb": args.c4_budget,
-                       "draws": [list(d[:3]) for d in taken], "units_per_step": units,
-                       "l2": "inputs larger than L2"},
+                                   "32 or 128 directions; seed 4), one graph launch per sub-batch" % tuple(args.c4_tiles),
+                       "problems": ndraws, "of_draws": len(draws), "sub_batches": len(batches),
+                       "device_budget_gb": args.c4_budget, "units_per_step": tot_units,
+                       "autotuned": not args.c4_no_tune, "l2": "inputs larger than L2"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_source": src,
                          "kernel": "whole batch (stage kernels and tallies of every problem)",
-                         "bytes_per_unit": balg_units / units},
-            "sequential": {"value": t_s * 1e6 / units, "unit": "ns", "ms_per_step": t_s,
+                         "bytes_per_unit": tot_balg / tot_units},
+            "sequential": {"value": ts_ms * 1e6 / tot_units, "unit": "ns", "ms_per_step": ts_ms,
                            "how": "the same contexts swept one after another (umt103_sweep_resident)"},
-            "wall_clock": {"batch_ms": w_b, "sequential_ms": w_s, "ratio": w_s / w_b,
+            "wall_clock": {"batch_ms": wb_ms, "sequential_ms": ws_ms, "ratio": ws_ms / wb_ms,
                            "how": "host time of each whole call (launch, wait, status checks); the batch "
                                   "graph is instantiated once and replayed (kept by umt103_batch_sweep)"},
+            "sub_batches": per_batch,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -498,6 +592,8 @@ def main():
     ap.add_argument("--tiles", type=int, default=None, help="tiles per axis (default 20, or 30 for --config 3)")
     ap.add_argument("--c4-budget", type=float, default=160.0,
                     help="--config 4: device memory (GB) the batch of draws may take")
+    ap.add_argument("--c4-max-batches", type=int, default=0, help="--config 4: time only the first N sub-batches")
+    ap.add_argument("--c4-no-tune", action="store_true", help="--config 4: skip the per-shape autotuning")
     ap.add_argument("--c4-tiles", type=int, nargs=2, default=(4, 16), metavar=("LO", "HI"),
                     help="--config 4: range of tiles per axis of the draws (default 4 16)")
     ap.add_argument("--config", type=int, default=2, choices=(2, 3, 4, 5),
@@ -508,6 +604,8 @@ def main():
     ap.add_argument("--no-ttc", action="store_true", help="skip the time-to-converge measurement")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 same-workload sweep figure")
     ap.add_argument("--no-learned", action="store_true", help="--config 5: skip the learned time-to-converge leg")
+    ap.add_argument("--shard", action="store_true",
+                    help="time the angle-sharded source-iteration step (directions split over the ranks)")
     ap.add_argument("--ttc-tiles", type=int, default=6, help="--config 5: tiles per axis of the time-to-converge mesh")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
     ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (precision as --precision)")
@@ -529,6 +627,13 @@ def main():
     if args.rz:
         if rank == 0:
             run_rz(args)
+        return
+    if args.shard:
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "--shard is timed on the GPU arm only"}))
+            return
+        run_shard(args, world, rank, local)
         return
 
     if args.impl == "reference":

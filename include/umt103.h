@@ -160,6 +160,22 @@ int umt103_set_source(const double *STotal);
 int umt103_sweep_resident(int savePsi, int precision);
 int umt103_get_phi(double *PhiTotal);
 
+/*
+ * Source iteration one step at a time, for a caller that owns the collective:
+ * with the directions split over ranks (one GPU each), every rank runs
+ * umt103_si_step (STotal = wtiso (sigma_s PhiTotal + q) built on the device,
+ * then a resident sweep of its directions), sums the device PhiTotal over
+ * ranks in place (e.g. an NCCL all-reduce on the pointer umt103_phi_device
+ * returns: nc*G FP64, valid until the context is released), and calls
+ * umt103_si_change for the relative L2 change since its last call.  This is
+ * the flux all-reduce of snac/SetSweep.F90:199 and rt/scat_prod.F90:81.
+ * umt103_set_external_source uploads q [nzones*G] once (NULL: none).
+ */
+int umt103_phi_device(double **phi, long long *count);
+int umt103_set_external_source(const double *q_ext);
+int umt103_si_step(int precision);
+int umt103_si_change(double *rel);
+
 /* Source iteration (rtmainsn / LinearSolver / ConvergenceTest).
  *
  * UMT_MIXED is defect correction: each outer step is one FP64 sweep of the

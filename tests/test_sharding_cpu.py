@@ -161,3 +161,77 @@ def test_rank_failure_ends_the_other_ranks_collective():
     assert res[1][0].startswith("RuntimeError: rank failure injected")
     assert res[0][0] != "finished"                   # the survivor learned of the failure
     assert res[0][1] == 3                            # in the iteration the failing rank left
+
+
+class OracleBufferSweeper(OracleSweeper):
+    """The device data plane's interface (DeviceSweeper) over the oracle: the
+    rank's PhiTotal lives in one persistent buffer (a host tensor here, the
+    library's device buffer on a GPU), the step builds the source from it and
+    overwrites it with this rank's partial flux, the change is taken against
+    the previous iterate."""
+
+    def __init__(self, prob, dirs):
+        import torch
+        super().__init__(prob, dirs)
+        m = prob.mesh
+        self.buf = torch.zeros(m.ncornr * prob.ngr, dtype=torch.float64)
+        self.prev = np.zeros(m.ncornr * prob.ngr)
+
+    def phi_tensor(self):
+        return self.buf
+
+    def step(self):
+        import torch
+        p, m = self.prob, self.prob.mesh
+        phi = self.buf.numpy().reshape(m.ncornr, p.ngr)
+        part = OracleSweeper.sweep(self, sharding.scattering_source(p, phi, p.q_ext))
+        self.buf.copy_(torch.from_numpy(part.ravel()))
+
+    def change(self):
+        cur = self.buf.numpy().copy()
+        d = np.linalg.norm(cur - self.prev)
+        n = np.linalg.norm(cur)
+        self.prev = cur
+        return d / n if n > 0 else 0.0
+
+
+def _rank_device_plane_main(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        prob = _problem()
+        dirs = sharding.direction_shards(len(prob.weight), world)[rank]
+        sw = OracleBufferSweeper(prob, dirs)
+        it, conv = sharding.source_iterate_device(sw, sharding.torch_allreduce_inplace(), rel_tol=1e-10,
+                                                  max_iters=300)
+        out.put((rank, sw.buf.numpy().copy(), it, conv))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_device_plane_sharded_iteration_matches_single_rank():
+    """source_iterate_device (in-place all-reduce of each rank's PhiTotal
+    buffer) over two gloo ranks gives the single-rank iteration."""
+    prob = _problem()
+    ref_phi, ref_it, ref_conv = sharding.source_iterate(OracleSweeper(prob, np.arange(len(prob.weight))), prob,
+                                                        lambda x: x, q_ext=prob.q_ext, rel_tol=1e-10,
+                                                        max_iters=300)
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_device_plane_main, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in procs:
+        r, phi, it, conv = out.get(timeout=300)
+        res[r] = (phi, it, conv)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert np.array_equal(res[0][0], res[1][0])
+    assert res[0][2] and res[0][1] == ref_it
+    got = res[0][0].reshape(ref_phi.shape)
+    assert float(np.max(np.abs(got - ref_phi)) / np.max(np.abs(ref_phi))) < 1e-12

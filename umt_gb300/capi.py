@@ -102,7 +102,8 @@ def load():
                   "umt103_mlp_init", "umt103_mlp_info", "umt103_mlp_get_params", "umt103_mlp_set_params",
                   "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect", "umt103_mlp_set_targets",
                   "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train", "umt103_autotune",
-                  "umt103_autotune_contexts", "umt103_gta_correction"):
+                  "umt103_autotune_contexts", "umt103_gta_correction", "umt103_phi_device",
+                  "umt103_set_external_source", "umt103_si_step", "umt103_si_change"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_mlp_finalize.restype = None
         _fp = C.POINTER(C.c_float)
@@ -130,7 +131,8 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_mlp_init", "umt103_mlp_finalize", "umt103_mlp_info", "umt103_mlp_get_params",
             "umt103_mlp_set_params", "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect",
             "umt103_mlp_set_targets", "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train",
-            "umt103_autotune", "umt103_autotune_contexts", "umt103_gta_correction"]
+            "umt103_autotune", "umt103_autotune_contexts", "umt103_gta_correction", "umt103_phi_device",
+            "umt103_set_external_source", "umt103_si_step", "umt103_si_change"]
 
 
 def check(rc):
@@ -378,6 +380,30 @@ class Library:
     def set_gta(self, max_krylov=10, tol=1e-4, spectrum=0):
         self.lib.umt103_set_gta.argtypes = [C.c_int, C.c_double, C.c_int]
         check(self.lib.umt103_set_gta(int(max_krylov), float(tol), int(spectrum)))
+
+    def phi_device(self):
+        """umt103_phi_device: (device address, element count) of PhiTotal."""
+        p, n = C.c_void_p(0), C.c_longlong(0)
+        check(self.lib.umt103_phi_device(C.byref(p), C.byref(n)))
+        return p.value, n.value
+
+    def set_external_source(self, q_ext=None):
+        q = _c(q_ext, np.float64)
+        check(self.lib.umt103_set_external_source(_d(q)))
+
+    def si_step(self, precision=UMT_FP64):
+        check(self.lib.umt103_si_step(int(precision)))
+
+    def si_change(self):
+        r = C.c_double(0.0)
+        check(self.lib.umt103_si_change(C.byref(r)))
+        return r.value
+
+    def schedule_info(self, angle):
+        """umt103_schedule_info: (hyperplanes, cycle-list corners) of one direction."""
+        h, n = C.c_int(0), C.c_int(0)
+        check(self.lib.umt103_schedule_info(int(angle), C.byref(h), C.byref(n)))
+        return h.value, n.value
 
     def gta_correction(self, PhiPrev):
         """umt103_gta_correction: (grey correction [nc], chi [nz, G], grey sweeps)."""

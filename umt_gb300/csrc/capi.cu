@@ -1380,6 +1380,59 @@ int umt103_source_iterate(const UmtSIParams *prm, UmtSIResult *res) {
   return conv ? 0 : set_error(UMT_ERR_NOTCONV, "not converged after %d iterations (rel change %.3e)", it, rel);
 }
 
+// ---- source iteration one step at a time, for a caller that owns the
+// collective (angle sharding: each rank sweeps its directions, then sums
+// PhiTotal over ranks in place on the device) ----
+int umt103_phi_device(double **phi, long long *count) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!phi) return set_error(UMT_ERR_ARG, "null output");
+  *phi = c.Phi;
+  if (count) *count = (long long)c.nc * c.G;
+  return 0;
+}
+
+int umt103_set_external_source(const double *q_ext) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  const size_t nzG = (size_t)c.nz * c.G;
+  if (!q_ext) { dfree(c.qExt); return 0; }
+  if (!c.qExt) TRY(dalloc(&c.qExt, nzG));
+  UMT_CUDA(cudaMemcpy(c.qExt, q_ext, nzG * 8, cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int umt103_si_step(int precision) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (c.rz) return set_error(UMT_ERR_STATE, "the context holds an RZ problem");
+  if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
+  if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
+  if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
+  TRY(launch_build_source(c, c.qExt));
+  TRY(launch_sweep_once(c, precision, true));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int umt103_si_change(double *rel) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (!rel) return set_error(UMT_ERR_ARG, "null output");
+  const size_t ncG = (size_t)c.nc * c.G;
+  if (!c.red) TRY(dalloc(&c.red, 16));
+  if (!c.PhiPrev) {
+    TRY(dalloc(&c.PhiPrev, ncG));
+    UMT_CUDA(cudaMemset(c.PhiPrev, 0, ncG * 8));
+  }
+  TRY(launch_change_norm(c, c.PhiPrev, c.red));
+  double h[3];
+  UMT_CUDA(cudaMemcpyAsync(h, c.red, 3 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  *rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
+  return 0;
+}
+
 int umt103_tally(const double *siga, double speed_light, UmtEnergyTally *t) {
   if (!cur().ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
   return umt103_tally_precision(siga, speed_light, cur().psi64[0] ? UMT_FP64 : UMT_FP32, t);

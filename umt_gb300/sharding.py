@@ -13,6 +13,14 @@ same way.
 The collective is passed in as a callable, so the same host logic runs over
 NCCL between GPUs (torch.distributed with device tensors) or over gloo on
 host tensors.
+
+Two data planes: `LibrarySweeper` + `source_iterate` move PhiTotal through
+the host each iteration (any collective, any device count); `DeviceSweeper`
++ `source_iterate_device` keep it on the GPU: the library builds the
+scattering source from PhiTotal on the device and sweeps (umt103_si_step),
+the collective sums the library's own PhiTotal buffer in place (a torch
+view of umt103_phi_device, no copy), and the change norm is taken on the
+device (umt103_si_change).
 """
 from __future__ import annotations
 
@@ -104,3 +112,70 @@ def source_iterate(sweeper, prob, allreduce: Callable[[np.ndarray], np.ndarray],
         if rel < rel_tol:
             return phi, it, True
     return phi, max_iters, False
+
+
+class CudaBuffer:
+    """A library-owned device buffer of FP64 values, exposed through the CUDA
+    array interface so that torch (or any consumer of the interface) can view
+    it without copying."""
+
+    def __init__(self, ptr: int, count: int):
+        self.__cuda_array_interface__ = {"shape": (int(count),), "typestr": "<f8", "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def torch_allreduce_inplace(group=None):
+    """In-place sum all-reduce of a tensor (NCCL for CUDA tensors, gloo for
+    host tensors)."""
+    import torch.distributed as dist
+
+    def reduce(t):
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        return t
+
+    return reduce
+
+
+class DeviceSweeper:
+    """This rank's directions with PhiTotal kept on this rank's GPU."""
+
+    def __init__(self, lib, prob, directions: np.ndarray, precision: int, flags: int = 8):
+        from . import capi
+        self.lib, self.prob, self.dirs, self.precision = lib, prob, np.asarray(directions), precision
+        m = prob.mesh
+        need = 2 if precision == capi.UMT_FP32 else 1
+        lib.init(m, prob.omega[self.dirs], prob.weight[self.dirs], prob.ngr, flags=flags | need)
+        lib.set_materials(prob.sigt, prob.sigs, prob.tau)
+        if prob.psi0 is not None:
+            lib.set_psi(prob.psi0[self.dirs], None)
+        lib.set_external_source(prob.q_ext)
+
+    def phi_tensor(self):
+        import torch
+        return torch.as_tensor(CudaBuffer(*self.lib.phi_device()), device="cuda")
+
+    def step(self):
+        self.lib.si_step(self.precision)
+
+    def change(self) -> float:
+        return self.lib.si_change()
+
+
+def source_iterate_device(sweeper, allreduce_inplace, rel_tol: float = 1e-8, max_iters: int = 200):
+    """Source iteration with the directions sharded over ranks and PhiTotal
+    on the device: step (source + sweep of this rank's directions), sum
+    PhiTotal over ranks in place, change norm.  Returns (iterations,
+    converged); the full PhiTotal is left in sweeper.phi_tensor()."""
+    import torch
+    phi = sweeper.phi_tensor()
+    sync = torch.cuda.synchronize if phi.is_cuda else (lambda: None)
+    phi.zero_()
+    sync()                                         # torch's stream before the library's
+    sweeper.change()                               # previous iterate := 0
+    for it in range(1, max_iters + 1):
+        sweeper.step()                             # returns with the library's stream drained
+        allreduce_inplace(phi)
+        sync()
+        if sweeper.change() < rel_tol:
+            return it, True
+    return max_iters, False
