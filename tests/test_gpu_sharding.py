@@ -72,7 +72,7 @@ def test_device_plane_two_shards_match_one_context(umtlib, precision, si_tol, to
             for cid, sw in zip(ids, sws):
                 umtlib.context_select(cid)
                 rel.append(sw.change())
-            assert rel[0] == rel[1]
+            assert abs(rel[0] - rel[1]) <= 1e-12 * max(rel[0], 1e-300)   # atomic reduction order
             return rel[0]
 
     pair = Pair()

@@ -378,9 +378,11 @@ __global__ void k_items2(size_t n, int nz, const uint32_t *items, const int *cOf
 // zones not yet placed; in each component of more than one zone, the root's
 // incoming faces from zones still on the search stack are cut and those
 // zones' corners go on the cycle list; a root left with no need starts the
-// next stage).  The search visits zones in increasing order and faces in
+// next hyperplane).  The search visits zones in increasing order and faces in
 // face order, depth first, as the recursive reference does; it keeps an
-// explicit stack so that deep meshes cannot overflow the host stack.
+// explicit stack so that deep meshes cannot overflow the host stack.  Every
+// cut is recorded, so that order_direction can give it the reference's
+// outcome.
 // ---------------------------------------------------------------------------
 struct DirGraph {
   int nz;
@@ -389,9 +391,12 @@ struct DirGraph {
   uint8_t *exitMask, *cyc;                      // [nz]
   bool exit(int z, int f) const { return (exitMask[z] >> f) & 1u; }
   void clear_exit(int z, int f) { exitMask[z] &= (uint8_t)~(1u << f); }
+  void set_exit(int z, int f) { exitMask[z] |= (uint8_t)(1u << f); }
 };
 
-static int seed_fallback(DirGraph &g, std::vector<int> &freed) {
+struct Cut { int from, face, root; };            // the edge from -> root across face `face` of `from`
+
+static int seed_fallback(DirGraph &g, std::vector<int> &freed, std::vector<Cut> &cuts) {
   int minNeed = g.nz, zoneID = -1;
   for (int z = 0; z < g.nz; ++z) {
     bool bdy = false;
@@ -405,6 +410,7 @@ static int seed_fallback(DirGraph &g, std::vector<int> &freed) {
     const int zo = g.zoneOpp[zoneID * UMT_MAXFACES + f], fo = g.faceOpp[zoneID * UMT_MAXFACES + f];
     if (zo >= 0) {
       g.cyc[zo] = 1;
+      if (g.exit(zo, fo)) cuts.push_back({zo, fo, zoneID});
       g.clear_exit(zo, fo);
     }
   }
@@ -412,7 +418,7 @@ static int seed_fallback(DirGraph &g, std::vector<int> &freed) {
   return 0;
 }
 
-static int break_cycles(DirGraph &g, std::vector<int> &freed) {
+static int break_cycles(DirGraph &g, std::vector<int> &freed, std::vector<Cut> &cuts) {
   const int nz = g.nz;
   std::vector<int> dfnum(nz, 0), lowlink(nz, 0), stk, breakList, tmp;
   std::vector<char> isnew(nz, 0), onstack(nz, 0);
@@ -449,6 +455,7 @@ static int break_cycles(DirGraph &g, std::vector<int> &freed) {
         g.cyc[zb] = 1;
         g.need[root] -= 1;
         g.clear_exit(zb, fb);
+        cuts.push_back({zb, fb, root});
         if (g.need[root] == 0) breakList.push_back(root);
       }
     }
@@ -487,6 +494,62 @@ static int break_cycles(DirGraph &g, std::vector<int> &freed) {
   return freed.empty() ? -1 : 0;
 }
 
+// One direction whose graph holds a cycle (or has no seed), ordered the way
+// the reference's sequential hyperplane loop orders it (snac/snnext.F90:
+// 109-195: the zones of a hyperplane one after another, each releasing the
+// zones across its exit faces in face order; findseeds when nothing starts;
+// cyclebreaker when the loop stalls, its freed zones in the order found).
+// That order decides what every zone reads across an edge the reference
+// cuts: the upstream zone's new flux when the upstream zone comes first, its
+// previous flux (the cycle list's) otherwise.  The schedule takes the same
+// decisions as dependency edges: a cut edge whose upstream zone comes first
+// stays an edge, any other is reversed.  Every edge then points forward in
+// the reference's order, so the direction's graph is acyclic, the wavefront
+// places it without a stall, and no two zones that read one another share a
+// stage.  The cycle flags (g.cyc) become the reference's cycle list.
+static int order_direction(DirGraph &g) {
+  const int nz = g.nz;
+  std::vector<int> need(g.need, g.need + nz);
+  std::vector<uint8_t> ex(g.exitMask, g.exitMask + nz);
+  DirGraph w{nz, g.zoneFaces, g.zoneOpp, g.faceOpp, need.data(), ex.data(), g.cyc};
+  std::vector<int> list, seq(nz, -1);
+  std::vector<Cut> cuts;
+  list.reserve(nz);
+  for (int z = 0; z < nz; ++z)
+    if (need[z] == 0) list.push_back(z);
+  if (list.empty() && seed_fallback(w, list, cuts)) return -1;
+  size_t head = 0;
+  while (list.size() < (size_t)nz) {
+    if (head == list.size()) {                    // stalled: break the cycles that hold it up
+      std::vector<int> freed;
+      if (break_cycles(w, freed, cuts)) return -1;
+      list.insert(list.end(), freed.begin(), freed.end());
+      continue;
+    }
+    const size_t end = list.size();
+    for (; head < end; ++head) {
+      const int z = list[head];
+      seq[z] = (int)head;
+      for (int f = 0; f < g.zoneFaces[z]; ++f) {
+        if (!w.exit(z, f)) continue;
+        const int zo = g.zoneOpp[z * UMT_MAXFACES + f];
+        if (zo < 0 || seq[zo] >= 0) continue;
+        if (--need[zo] == 0) list.push_back(zo);
+        else if (need[zo] < 0) return -1;
+      }
+    }
+  }
+  for (; head < list.size(); ++head) seq[list[head]] = (int)head;
+  for (const Cut &e : cuts) {
+    if (!g.exit(e.from, e.face) || seq[e.from] < seq[e.root]) continue;
+    g.clear_exit(e.from, e.face);                 // the root comes first: it reads the previous flux
+    g.need[e.root] -= 1;
+    g.set_exit(e.root, g.faceOpp[e.from * UMT_MAXFACES + e.face]);
+    g.need[e.from] += 1;
+  }
+  return 0;
+}
+
 // Host copies of the mesh connectivity the breaker needs.
 struct HostConn {
   std::vector<int> zoneFaces, zoneOpp, faceOpp, numCorner, cOffSet;
@@ -502,66 +565,35 @@ static int host_conn(Ctx &c, HostConn &h) {
   return 0;
 }
 
-int build_schedule(Ctx &c) {
+// The per-direction dependency graphs (snneed) and corner orders, from scratch.
+static int build_graphs(Ctx &c, const SchedArgs &p, int B) {
   Schedule &s = c.sch;
   const size_t n = (size_t)c.A * c.nz;
   UMT_CUDA(cudaMemsetAsync(s.need, 0, n * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.exitMask, 0, ((n + 3) & ~(size_t)3), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.cycZ, 0, n, c.stream));
+  k_need<<<B, 256, 0, c.stream>>>(p);
+  k_corner_order<<<B, 256, 0, c.stream>>>(p);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// The wavefront over every direction at once.  Returns 0 when every item was
+// placed, 1 when it stalled (a direction with a cycle, or without a seed).
+static int run_wavefront(Ctx &c, int B, int *stalledAt) {
+  Schedule &s = c.sch;
+  const size_t n = (size_t)c.A * c.nz;
   UMT_CUDA(cudaMemsetAsync(s.level, 0xff, n * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.stageCount, 0, (c.nz + 2) * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.stageOffset, 0, (c.nz + 2) * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.nHyper, 0, c.A * sizeof(int), c.stream));
   UMT_CUDA(cudaMemsetAsync(s.processed, 0, sizeof(unsigned long long), c.stream));
-  SchedArgs p{c.nz, c.nc, c.A, c.numCorner, c.cOffSet, c.zoneFaces, c.zoneOpp, c.faceOpp,
-              c.nCFaces, c.cEZ, c.CToFace, c.afp64, c.aez64, s.need, s.exitMask, s.bad, s.order, c.status, s.cycZ};
-  const int B = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
-  k_need<<<B, 256, 0, c.stream>>>(p);
-  k_corner_order<<<B, 256, 0, c.stream>>>(p);
-  UMT_CUDA(cudaGetLastError());
-  HostConn hc;
-  bool haveConn = false;
-  s.breaks = 0;
-  // directions without a seed (findseeds.F90:71-112)
-  {
-    int *cnt = nullptr;
-    UMT_CUDA(cudaMalloc((void **)&cnt, c.A * sizeof(int)));
-    std::vector<int> hcnt(c.A);
-    cudaError_t e = cudaMemsetAsync(cnt, 0, c.A * sizeof(int), c.stream);
-    if (e == cudaSuccess) {
-      k_seed_count<<<B, 256, 0, c.stream>>>(c.nz, c.A, s.need, cnt);
-      e = cudaMemcpyAsync(hcnt.data(), cnt, c.A * sizeof(int), cudaMemcpyDeviceToHost, c.stream);
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
-    cudaFree(cnt);
-    if (e != cudaSuccess) return set_error(-3, "seed count: %s", cudaGetErrorString(e));
-    for (int a = 0; a < c.A; ++a) {
-      if (hcnt[a] > 0) continue;
-      if (!haveConn) { TRY_RC(host_conn(c, hc)); haveConn = true; }
-      std::vector<int> need(c.nz);
-      std::vector<uint8_t> ex(c.nz), cy(c.nz);
-      const size_t o = (size_t)a * c.nz;
-      UMT_CUDA(cudaMemcpy(need.data(), s.need + o, c.nz * sizeof(int), cudaMemcpyDeviceToHost));
-      UMT_CUDA(cudaMemcpy(ex.data(), s.exitMask + o, c.nz, cudaMemcpyDeviceToHost));
-      UMT_CUDA(cudaMemcpy(cy.data(), s.cycZ + o, c.nz, cudaMemcpyDeviceToHost));
-      DirGraph g{c.nz, hc.zoneFaces.data(), hc.zoneOpp.data(), hc.faceOpp.data(), need.data(), ex.data(), cy.data()};
-      std::vector<int> freed;
-      if (seed_fallback(g, freed)) return set_error(-4, "direction %d has no zone to start from", a);
-      UMT_CUDA(cudaMemcpy(s.need + o, need.data(), c.nz * sizeof(int), cudaMemcpyHostToDevice));
-      UMT_CUDA(cudaMemcpy(s.exitMask + o, ex.data(), c.nz, cudaMemcpyHostToDevice));
-      UMT_CUDA(cudaMemcpy(s.cycZ + o, cy.data(), c.nz, cudaMemcpyHostToDevice));
-      ++s.breaks;
-    }
-  }
   UMT_CUDA(cudaMemcpyAsync(s.needInit, s.need, n * sizeof(int), cudaMemcpyDeviceToDevice, c.stream));
   k_seed<<<B, 256, 0, c.stream>>>(c.nz, c.A, s.need, s.bad, s.items, s.stageCount, s.level, s.processed);
   UMT_CUDA(cudaGetLastError());
-  // stages: launch in batches; a stall with items left is a mesh cycle,
-  // broken on the host for every direction it holds up
-  int h = 0;
-  const int batch = 32;
-  const int SB = 152 * 8;
+  const int batch = 32, SB = 152 * 8;
   unsigned long long placed = 0;
+  int h = 0;
   while (true) {
     for (int k = 0; k < batch && h < c.nz; ++k, ++h)
       k_stage<<<SB, 256, 0, c.stream>>>(h, c.nz, c.A, c.zoneFaces, c.zoneOpp, s.exitMask, s.bad, s.need,
@@ -569,52 +601,64 @@ int build_schedule(Ctx &c) {
     UMT_CUDA(cudaGetLastError());
     UMT_CUDA(cudaMemcpyAsync(&placed, s.processed, sizeof(placed), cudaMemcpyDeviceToHost, c.stream));
     UMT_CUDA(cudaStreamSynchronize(c.stream));
-    if (placed == n) break;
-    std::vector<int> cnt(h + 1), off(h + 1);
+    if (placed == n) return 0;
+    std::vector<int> cnt(h + 1);
     UMT_CUDA(cudaMemcpy(cnt.data(), s.stageCount, (h + 1) * sizeof(int), cudaMemcpyDeviceToHost));
-    UMT_CUDA(cudaMemcpy(off.data(), s.stageOffset, (h + 1) * sizeof(int), cudaMemcpyDeviceToHost));
-    int h0 = -1;
-    for (int k = 1; k <= h; ++k)
-      if (cnt[k] == 0) { h0 = k; break; }
-    if (h0 < 0) {
-      if (h >= c.nz) return set_error(-4, "schedule: %llu of %zu items placed after %d stages", placed, n, h);
-      continue;                                   // still progressing
-    }
-    // stalled: stage h0 is empty and items remain
-    if (!haveConn) { TRY_RC(host_conn(c, hc)); haveConn = true; }
-    std::vector<int> need(n), lev(n);
-    std::vector<uint8_t> ex(n), cy(n), bad(n);
-    UMT_CUDA(cudaMemcpy(need.data(), s.need, n * sizeof(int), cudaMemcpyDeviceToHost));
+    int h0 = cnt[0] == 0 ? 0 : -1;
+    for (int k = 1; k <= h && h0 < 0; ++k)
+      if (cnt[k] == 0) h0 = k;
+    if (h0 >= 0) { *stalledAt = h0; return 1; }
+    if (h >= c.nz) return set_error(-4, "schedule: %llu of %zu items placed after %d stages", placed, n, h);
+  }
+}
+
+int build_schedule(Ctx &c) {
+  Schedule &s = c.sch;
+  const size_t n = (size_t)c.A * c.nz;
+  SchedArgs p{c.nz, c.nc, c.A, c.numCorner, c.cOffSet, c.zoneFaces, c.zoneOpp, c.faceOpp,
+              c.nCFaces, c.cEZ, c.CToFace, c.afp64, c.aez64, s.need, s.exitMask, s.bad, s.order, c.status, s.cycZ};
+  const int B = (int)std::min<size_t>((n + 255) / 256, 152 * 32);
+  TRY_RC(build_graphs(c, p, B));
+  HostConn hc;
+  bool haveConn = false;
+  s.breaks = 0;
+  int h0 = 0;
+  int rc = run_wavefront(c, B, &h0);
+  if (rc < 0) return rc;
+  if (rc == 1) {
+    // The directions left unplaced hold a cycle (or have no seed).  Their
+    // graphs are rebuilt and put in the reference's sequential order on the
+    // host; the wavefront then runs again over every direction.
+    std::vector<int> lev(n);
     UMT_CUDA(cudaMemcpy(lev.data(), s.level, n * sizeof(int), cudaMemcpyDeviceToHost));
-    UMT_CUDA(cudaMemcpy(ex.data(), s.exitMask, n, cudaMemcpyDeviceToHost));
-    UMT_CUDA(cudaMemcpy(cy.data(), s.cycZ, n, cudaMemcpyDeviceToHost));
-    UMT_CUDA(cudaMemcpy(bad.data(), s.bad, n, cudaMemcpyDeviceToHost));
-    std::vector<uint32_t> newItems;
+    std::vector<int> cyclic;
     for (int a = 0; a < c.A; ++a) {
       const size_t o = (size_t)a * c.nz;
-      bool left = false;
-      for (int z = 0; z < c.nz && !left; ++z) left = lev[o + z] < 0;
-      if (!left) continue;
-      DirGraph g{c.nz, hc.zoneFaces.data(), hc.zoneOpp.data(), hc.faceOpp.data(), need.data() + o, ex.data() + o,
-                 cy.data() + o};
-      std::vector<int> freed;
-      if (break_cycles(g, freed))
-        return set_error(-4, "direction %d: a dependency cycle could not be broken", a);
-      for (int z : freed) {
-        newItems.push_back((uint32_t)(o + z) | (bad[o + z] ? 0x80000000u : 0u));
-        lev[o + z] = h0;
-      }
+      for (int z = 0; z < c.nz; ++z)
+        if (lev[o + z] < 0) { cyclic.push_back(a); break; }
     }
-    if (newItems.empty()) return set_error(-4, "schedule stalled with no cycle to break");
-    ++s.breaks;
-    const int nn = (int)newItems.size();
-    UMT_CUDA(cudaMemcpy(s.need, need.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-    UMT_CUDA(cudaMemcpy(s.level, lev.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-    UMT_CUDA(cudaMemcpy(s.exitMask, ex.data(), n, cudaMemcpyHostToDevice));
-    UMT_CUDA(cudaMemcpy(s.cycZ, cy.data(), n, cudaMemcpyHostToDevice));
-    UMT_CUDA(cudaMemcpy(s.items + off[h0], newItems.data(), nn * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    UMT_CUDA(cudaMemcpy(s.stageCount + h0, &nn, sizeof(int), cudaMemcpyHostToDevice));
-    h = h0;                                       // the wavefront resumes from the freed zones
+    lev.clear();
+    lev.shrink_to_fit();
+    TRY_RC(build_graphs(c, p, B));
+    TRY_RC(host_conn(c, hc));
+    haveConn = true;
+    std::vector<int> need(c.nz);
+    std::vector<uint8_t> ex(c.nz), cy(c.nz);
+    for (int a : cyclic) {
+      const size_t o = (size_t)a * c.nz;
+      UMT_CUDA(cudaMemcpy(need.data(), s.need + o, c.nz * sizeof(int), cudaMemcpyDeviceToHost));
+      UMT_CUDA(cudaMemcpy(ex.data(), s.exitMask + o, c.nz, cudaMemcpyDeviceToHost));
+      UMT_CUDA(cudaMemcpy(cy.data(), s.cycZ + o, c.nz, cudaMemcpyDeviceToHost));
+      DirGraph g{c.nz, hc.zoneFaces.data(), hc.zoneOpp.data(), hc.faceOpp.data(), need.data(), ex.data(), cy.data()};
+      if (order_direction(g)) return set_error(-4, "direction %d: a dependency cycle could not be broken", a);
+      UMT_CUDA(cudaMemcpy(s.need + o, need.data(), c.nz * sizeof(int), cudaMemcpyHostToDevice));
+      UMT_CUDA(cudaMemcpy(s.exitMask + o, ex.data(), c.nz, cudaMemcpyHostToDevice));
+      UMT_CUDA(cudaMemcpy(s.cycZ + o, cy.data(), c.nz, cudaMemcpyHostToDevice));
+    }
+    s.breaks = (int)cyclic.size();
+    rc = run_wavefront(c, B, &h0);
+    if (rc < 0) return rc;
+    if (rc == 1) return set_error(-4, "schedule stalled at stage %d after the cycles were ordered", h0);
   }
   {
     const int B2 = (int)std::min<size_t>((n + 255) / 256, 152 * 32);

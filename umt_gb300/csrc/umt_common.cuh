@@ -45,7 +45,7 @@ struct Schedule {
   long long *cycRow = nullptr;    // [nCyc] a*nc + c
   long long nCyc = 0;
   std::vector<long long> hCycOff; // [A+1] per-direction offsets into cycRow
-  int breaks = 0;                 // cycle-breaker passes the build needed
+  int breaks = 0;                 // directions the build ordered on the host (a cycle or no seed)
 };
 
 struct Ctx {
