@@ -51,6 +51,38 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
+// Bulk (TMA 1-D) copies global -> shared completing on an mbarrier: one
+// thread moves a whole contiguous range (16-byte aligned, a multiple of 16
+// bytes) and the team waits on the barrier's first phase.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init_one(uint64_t *b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(b)) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_pol(void *dst, const void *src, uint32_t bytes, uint64_t *b,
+                                              unsigned long long pol) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(b)), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(b)) : "memory");
+}
+// Wait for the barrier's phase 0; gives up after 2^22 polls and returns false.
+__device__ __forceinline__ bool mbar_wait_phase0(uint64_t *b) {
+  for (int i = 0; i < (1 << 22); ++i) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(ok) : "r"(smem_addr(b)) : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
 // Programmatic dependent launch: allow the next kernel of the stream to start

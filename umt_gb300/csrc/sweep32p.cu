@@ -30,8 +30,8 @@
 // been staged no further synchronisation is needed.
 //
 // Memory round trips per zone: (1) header; (2) program, previous flux and
-// source of every corner (asynchronous copies), cross sections; (3) every
-// upwind flux.  The intra-zone solve pulls from upstream corners in the order
+// source of every corner (three bulk copies by one lane onto an mbarrier),
+// cross sections; (3) every upwind flux.  The intra-zone solve pulls from upstream corners in the order
 // the reference pushes to downstream ones, so every FMA chain of the solve is
 // the reference's.
 #include "umt_common.cuh"
@@ -50,13 +50,13 @@ struct ProgP {
   uint32_t nzMagic;                     // a = (it * nzMagic) >> nzShift equals it / nz for it < 2^31
   int nzShift;
   const uint4 *hdr;
-  const int *stageOffset, *stageCount;
   const uint4 *prog;
   const float *Sigt, *STotal;
   float tau;
   const float *psi_old;
   float *psi_new, *psiB;
   double *const *psibOut;               // device word: FP64 copy of the exiting PsiB rows, or null
+  unsigned *status;                     // device status word (a copy that never completed)
 };
 
 template <int NP>
@@ -84,7 +84,7 @@ __host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 
 // WT: also write the exiting rows, in FP64, to *p.psibOut (the variant used
 // by calls that return PsiB to the host; resident sweeps run the other).
 template <int GT, int GPL, bool WT>
-__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, int stage) {
+__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, int off, int nItems) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
   constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
   constexpr int G = GT * GPL;
@@ -94,19 +94,20 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   // stage's finish and run their independent first two round trips.
   pdl_launch_dependents();
   const int k = blockIdx.x * TEAMS + team;
-  if (k >= p.stageCount[stage]) return;            // whole teams leave together
+  if (k >= nItems) return;                         // whole teams leave together
   const unsigned tm = team_mask(GT, tid);
   const int g0 = lane * GPL;
-  // Row c of Q (later the solved psi) at c*RP, row c of S (running source) at
-  // c*RP + G: a team's window of one row lies in the same banks whatever the
-  // corner, and consecutive teams are G banks apart (team stride), so the
-  // teams sharing a shared-memory wavefront never collide.
-  constexpr int RP = pair_stride(G);
+  // The team's Q rows (later the solved psi) [8][G], then its S rows (running
+  // source) [8][G], each block a contiguous image of the HBM rows it is copied
+  // from.  Consecutive teams are G banks apart (team stride), so the teams
+  // sharing a shared-memory wavefront read disjoint banks.
+  constexpr int RP = G;
+  __shared__ __align__(8) uint64_t sBar[TEAMS];
   float *sQ = reinterpret_cast<float *>(smem4) + (size_t)team * p.tstride;
-  float *sS = sQ + G;
+  float *sS = sQ + 8 * G;
   unsigned char *sB = reinterpret_cast<unsigned char *>(smem4) + (size_t)TEAMS * p.tstride * 4 +
                       (size_t)team * p.bstride;
-  const uint4 h = p.hdr[p.stageOffset[stage] + k];
+  const uint4 h = p.hdr[off + k];
   const bool bad = (h.x >> 31) != 0;
   const uint32_t it = h.x & 0x7fffffffu;
   const int a = (int)(((unsigned long long)it * p.nzMagic) >> p.nzShift);
@@ -118,24 +119,38 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   float *psiNew = p.psi_new + abase * G + g0;
   float *psiBA = p.psiB + (size_t)a * p.nb * G + g0;
   // ---- round trip 2: program, previous flux, source, cross sections ----
-  {
-    // the program and the previous flux are read once per sweep: evict-first
+  // One lane moves the program and the corners' previous flux and source
+  // rows, each contiguous in HBM, with bulk copies on the team's mbarrier.
+  // The program and the previous flux are read once per sweep: evict-first.
+  // Rows narrower than 16 bytes (G < 4) go lane by lane.
+  constexpr bool BULK_ROWS = (G * 4) % 16 == 0;
+  if (lane == 0) {
     const unsigned long long once = l2_evict_first_policy();
-    const uint4 *src = p.prog + h.z;
-    for (int e = lane; e < nch; e += GT) cp_async16_cg_pol(sB + 16 * e, src + e, once);
+    const uint32_t rows = (uint32_t)(nC * G * 4);
+    mbar_init_one(&sBar[team]);
+    mbar_expect_tx(&sBar[team], (uint32_t)nch * 16u + (BULK_ROWS ? 2u * rows : 0u));
+    bulk_copy_pol(sB, p.prog + h.z, (uint32_t)nch * 16u, &sBar[team], once);
+    if constexpr (BULK_ROWS) {
+      bulk_copy_pol(sQ, p.psi_old + (abase + c0) * G, rows, &sBar[team], once);
+      bulk_copy(sS, p.STotal + (size_t)c0 * G, rows, &sBar[team]);
+    }
+  }
+  if constexpr (!BULK_ROWS) {
     const float *po = p.psi_old + (abase + c0) * G + g0;
     const float *st = p.STotal + (size_t)c0 * G + g0;
-#pragma unroll
-    for (int c = 0; c < UMT_MAXCORNER; ++c)
-      if (c < nC) {
-        cp_async_pol(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4, once);
-        cp_async(sS + c * RP + g0, st + (size_t)c * G, GPL * 4);
-      }
+    for (int c = 0; c < nC; ++c) {
+      cp_async(sQ + c * RP + g0, po + (size_t)c * G, GPL * 4);
+      cp_async(sS + c * RP + g0, st + (size_t)c * G, GPL * 4);
+    }
   }
   float2 sg[NP];
   ldg2<NP>(p.Sigt + (size_t)z * G + g0, sg);
-  cp_async_wait_all();
-  __syncwarp(tm);
+  if constexpr (!BULK_ROWS) cp_async_wait_all();
+  __syncwarp(tm);                                  // the barrier is initialised before anyone waits on it
+  if (!mbar_wait_phase0(&sBar[team])) {            // a copy that never completed: report, leave
+    atomicOr(p.status, UMT_DEV_TIMEOUT);
+    return;
+  }
   const uint32_t *W = reinterpret_cast<const uint32_t *>(sB);
   const uint32_t cnt = W[0], pcnt = W[1];
   const int nA = cnt & 31, nB = (cnt >> 5) & 31, nE = (cnt >> 10) & 31, nX = (cnt >> 15) & 31,
@@ -704,10 +719,10 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   p.tstride = team_stride_p(c.G);
   p.bstride = blob_stride_p(c.progMaxChunks);
   p.hdr = (const uint4 *)c.hdr32; p.prog = (const uint4 *)c.prog32;
-  p.stageOffset = c.sch.stageOffset; p.stageCount = c.sch.stageCount;
   p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = c.homog32 ? 0.f : (float)c.tau;
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.homog32 ? c.psiB32h : c.psiB32;
   p.psibOut = c.psibOut;
+  p.status = c.status;
   const int TEAMS = P32_NT / GT;
   const size_t smem = (size_t)TEAMS * ((size_t)p.tstride * 4 + p.bstride);
   // Stage 0 follows the source conversion with ordinary stream order; every
@@ -721,7 +736,7 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   cfg.stream = c.stream;
 #define UMT_LAUNCHP(gt, gpl)                                                                   \
   if (GT == gt && GPL == gpl) {                                                                \
-    void (*kern)(ProgP, int) = c.wantExitsThrough ? k_sweep32p<gt, gpl, true>                  \
+    void (*kern)(ProgP, int, int) = c.wantExitsThrough ? k_sweep32p<gt, gpl, true>                  \
                                                   : k_sweep32p<gt, gpl, false>;                \
     if (c.wantExitsThrough) {                                                                  \
       const int rq = enqueue_psib_chunks(c);                                                   \
@@ -735,7 +750,7 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
       cfg.gridDim = dim3((c.sch.hCount[s] + TEAMS - 1) / TEAMS);                               \
       cfg.attrs = s > 0 && c.usePDL ? pdl : nullptr;                                           \
       cfg.numAttrs = s > 0 && c.usePDL ? 1 : 0;                                                \
-      UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p, s));                                          \
+      UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p, c.sch.hOffset[s], c.sch.hCount[s]));                                          \
     }                                                                                          \
     if (c.wantExitsThrough) {                                                                  \
       const int rq = wait_psib_chunks(c, c.sch.nStages);                                       \
