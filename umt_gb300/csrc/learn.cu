@@ -258,16 +258,21 @@ __global__ void __launch_bounds__(MLP_NT, 1) k_mlp_backward(MlpNet net, MlpAct a
 
 // ---------------------------------------------------------------------------
 // Weight gradients: for layer l (blockIdx.y) and a chunk of the batch
-// (blockIdx.x), D = A B^T over the chunk's rows, then added to grad:
+// (blockIdx.x), D = A B^T over the chunk's rows, stored as the chunk's
+// partial tile; k_mlp_wreduce sums the chunks in chunk order, so a gradient
+// does not depend on the order in which CTAs finish:
 //   l = 0..2: A = dZ_l^T [128 out][rows], B = X_l^T [in][rows]  -> dW_l[out][in]
 //   l = 3:    A = H3^T  [128 in][rows],   B = dO^T [N4][rows]  -> dW4[o][h] transposed
+// Partial tile (l, chunk) holds D[m][n] at ((l*nchunk + chunk)*128 + m)*MLP_WPN + n.
 // ---------------------------------------------------------------------------
+constexpr int MLP_WPN = 256;                   // widest B operand (rows of sB)
+constexpr int MLP_WCHUNKS = 32;                // most chunks per layer
 static size_t wgrad_smem() { return (size_t)MLP_H * MLP_H * 2 + (size_t)256 * MLP_H * 2 + 16; }
 
 struct MlpGradOff { long w[4], b[4]; };
 
-__global__ void __launch_bounds__(MLP_NT, 1) k_mlp_wgrad(MlpNet net, MlpAct act, MlpGradOff off, float *grad,
-                                                         int chunk, unsigned *status) {
+__global__ void __launch_bounds__(MLP_NT, 1) k_mlp_wgrad(MlpNet net, MlpAct act, float *part, int chunk,
+                                                         unsigned *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char *sA = smem;
   unsigned char *sB = sA + (size_t)MLP_H * MLP_H * 2;
@@ -305,20 +310,13 @@ __global__ void __launch_bounds__(MLP_NT, 1) k_mlp_wgrad(MlpNet net, MlpAct act,
     tc_fence_after();
     const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
     const int m = warp * 32 + lane;
+    float *dst = part + ((size_t)(l * gridDim.x + blockIdx.x) * MLP_H + m) * MLP_WPN;
     for (int j0 = 0; j0 < N; j0 += 16) {
       float v[16];
       tmem_ld16(tl + (uint32_t)j0, v);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int n = j0 + i;
-        if (l == 0) {
-          if (n < net.F) atomicAdd(grad + off.w[0] + (long)m * net.F + n, v[i]);
-        } else if (l < 3) {
-          atomicAdd(grad + off.w[l] + (long)m * MLP_H + n, v[i]);
-        } else if (n < net.G) {
-          atomicAdd(grad + off.w[3] + (long)n * MLP_H + m, v[i]);
-        }
-      }
+      for (int i = 0; i < 16; i += 4)
+        *reinterpret_cast<float4 *>(dst + j0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
     }
   } else {
     if (tid == 0) atomicOr(status, UMT_DEV_TIMEOUT);
@@ -333,6 +331,23 @@ __global__ void __launch_bounds__(MLP_NT, 1) k_mlp_wgrad(MlpNet net, MlpAct act,
 }
 
 // bias gradients: row sums of dZ_l^T (l < 3) and of dO^T (the output layer)
+// grad (weights) = sum over the chunks' partial tiles, in chunk order
+__global__ void k_mlp_wreduce(MlpNet net, MlpGradOff off, const float *part, int nchunk, float *grad) {
+  const long total = 4l * MLP_H * MLP_WPN;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const int l = (int)(t / ((long)MLP_H * MLP_WPN));
+    const int m = (int)(t / MLP_WPN % MLP_H), n = (int)(t % MLP_WPN);
+    float *dst;
+    if (l == 0) dst = n < net.F ? grad + off.w[0] + (long)m * net.F + n : nullptr;
+    else if (l < 3) dst = n < MLP_H ? grad + off.w[l] + (long)m * MLP_H + n : nullptr;
+    else dst = n < net.G ? grad + off.w[3] + (long)n * MLP_H + m : nullptr;
+    if (!dst) continue;
+    float s = 0.f;
+    for (int c = 0; c < nchunk; ++c) s += part[((size_t)(l * nchunk + c) * MLP_H + m) * MLP_WPN + n];
+    *dst = s;
+  }
+}
+
 __global__ void k_mlp_bgrad(MlpNet net, MlpAct act, MlpGradOff off, float *grad) {
   const int warpsPer = blockDim.x / 32;
   const int w = blockIdx.x * warpsPer + (threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -618,6 +633,7 @@ struct Mlp {
   int G = 0, F = 0, K1 = 0, N4 = 0;
   MlpParamOff po{};
   float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+  float *wpart = nullptr;                       // weight-gradient partial tiles [4][chunks][128][MLP_WPN]
   __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr, *W2T = nullptr, *W3T = nullptr, *W4T = nullptr;
   long step = 0;
   // batch workspace
@@ -646,7 +662,7 @@ static void mlp_free_workspace(Mlp &n) {
 
 static void mlp_free(Mlp &n) {
   mlp_free_workspace(n);
-  free_n(n.p); free_n(n.g); free_n(n.m); free_n(n.v);
+  free_n(n.p); free_n(n.g); free_n(n.m); free_n(n.v); free_n(n.wpart);
   free_n(n.W1); free_n(n.W2); free_n(n.W3); free_n(n.W4); free_n(n.W2T); free_n(n.W3T); free_n(n.W4T);
   free_n(n.red); free_n(n.status);
   free_n(n.Xd); free_n(n.Dd); free_n(n.Pd); free_n(n.Td); free_n(n.Wd);
@@ -747,10 +763,15 @@ static int mlp_backward(Mlp &n, int rows) {
   const MlpAct act = act_view(n, rows);
   const int tiles = rows / 128;
   k_mlp_backward<<<std::max(1, std::min(tiles, 152)), MLP_NT, backward_smem(n.N4), n.stream>>>(net, act, n.status);
-  UMT_CUDA(cudaMemsetAsync(n.g, 0, n.po.n * sizeof(float), n.stream));
-  const int chunk = std::max(128, (rows / 128 + 31) / 32 * 128);       // at most 32 chunks per layer
-  dim3 grid((rows + chunk - 1) / chunk, 4);
-  k_mlp_wgrad<<<grid, MLP_NT, wgrad_smem(), n.stream>>>(net, act, grad_off(n), n.g, chunk, n.status);
+  if (!n.wpart) {
+    int rc = malloc_n(&n.wpart, (size_t)4 * MLP_WCHUNKS * MLP_H * MLP_WPN);
+    if (rc) return rc;
+  }
+  const int chunk = std::max(128, (rows / 128 + MLP_WCHUNKS - 1) / MLP_WCHUNKS * 128);
+  const int nchunk = (rows + chunk - 1) / chunk;
+  dim3 grid(nchunk, 4);
+  k_mlp_wgrad<<<grid, MLP_NT, wgrad_smem(), n.stream>>>(net, act, n.wpart, chunk, n.status);
+  k_mlp_wreduce<<<512, 256, 0, n.stream>>>(net, grad_off(n), n.wpart, nchunk, n.g);
   const int nrow = 3 * MLP_H + n.G;
   k_mlp_bgrad<<<(nrow + 7) / 8, 256, 0, n.stream>>>(net, act, grad_off(n), n.g);
   UMT_CUDA(cudaGetLastError());
