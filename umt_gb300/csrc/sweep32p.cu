@@ -147,8 +147,9 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, 
   ldg2<NP>(p.Sigt + (size_t)z * G + g0, sg);
   if constexpr (!BULK_ROWS) cp_async_wait_all();
   __syncwarp(tm);                                  // the barrier is initialised before anyone waits on it
-  if (!mbar_wait_phase0(&sBar[team])) {            // a copy that never completed: report, leave
-    atomicOr(p.status, UMT_DEV_TIMEOUT);
+  if (!mbar_wait_phase0(&sBar[team])) {            // a copy that never completed: report, give the
+    atomicOr(p.status, UMT_DEV_TIMEOUT);           // copies in flight one more bounded wait, leave
+    mbar_wait_phase0(&sBar[team]);
     return;
   }
   const uint32_t *W = reinterpret_cast<const uint32_t *>(sB);
