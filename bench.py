@@ -15,19 +15,24 @@ stand in for the reference's problem; there is no dataset.
 --config 3 is the larger scattering problem: 30^3 tiles, four materials by
 tile (seed 3), total opacity log-uniform on [1e-3, 1e3], scattering ratio up
 to 0.9; its sweep is timed without the time-to-converge run, whose FP64
-flux buffers (2 x 78 GB) would not fit beside the FP32 ones.  --config 5 is the strongly scattering 32-group problem: 20^3 tiles,
-total opacity log-uniform on [1, 1e3] per zone and group (seed 5), scattering
-ratio uniform on [0.95, 0.999]; its sweep is timed, without the
-time-to-converge run (plain source iteration needs hundreds of iterations at
-these ratios).  --config 4 sweeps a batch of independent problems of uneven
-size from one graph launch (tiles per axis U{4..16}, 4 to 64 groups, 32 or
-128 directions; seed 4), the draws that fit in --c4-budget GB of device
-memory, against the same contexts swept one after another.  --rz times the 2-D RZ sweep instead (200 x 200 quadrilaterals, 144
-directions, 16 groups).
+flux buffers (2 x 78 GB) would not fit beside the FP32 ones.  --config 5 is
+the strongly scattering 32-group problem: 20^3 tiles, total opacity
+log-uniform on [1, 1e3] per zone and group (seed 5), scattering ratio uniform
+on [0.95, 0.999]; its sweep is timed, and its time-to-converge leg runs the
+same distribution on --ttc-tiles tiles per axis: plain FP64 source iteration
+against FP64 and mixed FP64/FP32 iteration with the learned correction
+(trained first on seeded problems by the library's own kernels).  --config 4
+sweeps all 64 independent problems of uneven size (tiles per axis U{4..16},
+4 to 64 groups, 32 or 128 directions; seed 4) in sub-batches that fit in
+--c4-budget GB of device memory, each sub-batch from one graph launch,
+against the same contexts swept one after another.  --rz times the 2-D RZ
+sweep instead (200 x 200 quadrilaterals, 144 directions, 16 groups).
 
-Multi-GPU: the sweep of one problem does not shard here, so N GPUs run N
-independent replicas (one process per GPU, launched by torchrun); value is
-aggregated over all replicas (units of all ranks / max time over ranks).
+Multi-GPU: by default N GPUs run N independent replicas of the sweep (one
+process per GPU, launched by torchrun); value is aggregated over all
+replicas (units of all ranks / max time over ranks).  --shard instead splits
+one problem's directions over the ranks and times a source-iteration step
+with PhiTotal all-reduced in place on the devices.
 
 --impl reference times the reference algorithm on the host cores: the C++
 restatement of SweepUCBxyz/SetSweep (oracle/), FP64, OpenMP over directions
@@ -608,6 +613,8 @@ def main():
                     help="time the angle-sharded source-iteration step (directions split over the ranks)")
     ap.add_argument("--ttc-tiles", type=int, default=6, help="--config 5: tiles per axis of the time-to-converge mesh")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
+    ap.add_argument("--gta-solver", type=int, default=1, choices=(1, 2),
+                    help="with --gta: 1 grey + stretched-TSA sweeps, 2 grey sweep + per-zone direct solve")
     ap.add_argument("--rz", action="store_true", help="time the 2-D RZ sweep instead (precision as --precision)")
     ap.add_argument("--rz-cells", type=int, default=200, help="RZ mesh: cells per direction")
     args = ap.parse_args()
@@ -767,7 +774,11 @@ def main():
     if world == 1 and prec == capi.UMT_FP32 and fp64_ok:
         line["fp64"] = fp64_sweep_figure(lib, prob, units)
     if world == 1 and not args.no_ttc:
+        if args.gta:
+            lib.set_gta_solver(args.gta_solver)
         line["time_to_converge"] = time_to_converge(lib, prob, use_gta=args.gta)
+        if args.gta:
+            line["time_to_converge"]["gta_solver"] = args.gta_solver
     if world == 1 and args.config == 5 and not args.no_learned:
         line["time_to_converge"] = ttc_learned(args, lib)
     if not args.no_cpu_baseline and world == 1:

@@ -229,6 +229,18 @@ int umt103_source_iterate(const UmtSIParams *params, UmtSIResult *result);
  * weighted by 1/(1-c) per group). */
 int umt103_set_gta(int max_krylov, double tol, int spectrum);
 
+/* GTA solver (Teton's Size%useNewGTASolver, driver option gta_kernel):
+ * UMT_GTA_TSA (1, the reference's default) applies the grey operator as a
+ * grey S2 sweep plus a stretched-TSA sweep (rt/GreySweep.F90 GreySweep);
+ * UMT_GTA_ZONE (2) as one grey sweep followed by a direct solve of each
+ * zone's local scattering with the zone's transfer matrix
+ * (rt/GreySweep.F90 GreySweepNEW, snac/InitSweepGreyUCBxyz.F90,
+ * snac/UpdateScalarIntensity.F90).  Both feed the same BiCGStab
+ * (rt/GTASolver.F90). */
+#define UMT_GTA_TSA 1
+#define UMT_GTA_ZONE 2
+int umt103_set_gta_solver(int solver);
+
 /* The grey correction of one source iteration, not applied: with the
  * context's current PhiTotal and the previous iterate PhiPrev [ncornr*G], the
  * spectrum chi [nzones*G] (may be NULL) and the grey correction [ncornr]

@@ -167,3 +167,44 @@ def test_gta_restatement_properties():
     lhs = gp.sweep(sig, 2.0 * a + 3.0 * b)
     rhs = 2.0 * gp.sweep(sig, a) + 3.0 * gp.sweep(sig, b)
     assert np.abs(lhs - rhs).max() <= 1e-13 * np.abs(rhs).max()
+
+
+def test_gta_zone_solver_restatement():
+    """The restatement of the newer grey solver (InitSweepGreyUCBxyz,
+    SweepGreyUCBxyzKernelNew, ScalarIntensityDecompose/Solve): its literal
+    grey sweep equals the oracle's C++ sweep; the inflow part PhiInc it
+    accumulates equals tPhi - TT TsaSource (the identity the device uses);
+    the LU solve inverts A = I - TT wtiso sigma_s; and at a tight tolerance
+    the newer and the older solver reach the same grey correction."""
+    from oracle import gta_oracle as go
+    from umt_gb300.problems import synthetic_problem
+    prob = synthetic_problem((2, 2, 1), 2, 2, 4, seed=41, sigt_range=(0.5, 50.0), c_range=(0.5, 0.95),
+                             time_dependent=True)
+    m = prob.mesh
+    rng = np.random.default_rng(42)
+    phi = rng.uniform(0.5, 1.5, size=(m.ncornr, 4))
+    prev = phi * rng.uniform(0.9, 1.1, size=phi.shape)
+    gp = go.GreyProblem(m)
+    _, gt, gs = go.spectrum(m, gp.geo[2], prob.sigt, prob.sigs, prob.tau, phi, prev)
+    gtc, gsc = gt[m.cToZone], gs[m.cToZone]
+    TT = go.init_grey_tt(gp, gtc)
+    tsa = rng.uniform(0.1, 1.0, m.ncornr)
+    tphi, pinc = go.grey_sweep_new(gp, gtc, tsa)
+    ref = gp.sweep(gt, tsa)
+    assert np.abs(tphi - ref).max() <= 1e-14 * np.abs(ref).max()
+    alt = tphi.copy()
+    for z in range(m.nzones):
+        c0, nC = m.cOffSet[z], m.numCorner[z]
+        alt[c0:c0 + nC] -= TT[c0:c0 + nC, :nC] @ tsa[c0:c0 + nC]
+    assert np.abs(alt - pinc).max() <= 1e-13 * np.abs(pinc).max()
+    z = 3
+    c0, nC = m.cOffSet[z], m.numCorner[z]
+    A = np.eye(nC) - TT[c0:c0 + nC, :nC] * (go.WTISO * gsc[c0:c0 + nC])[None, :]
+    b = rng.uniform(size=nC)
+    x = np.array(go.zone_solve(go.zone_decompose(m, TT, gsc, z), b))
+    assert np.abs(A @ x - b).max() <= 1e-13 * np.abs(b).max()
+    args = (m, np.ascontiguousarray(prob.sigt), np.ascontiguousarray(prob.sigs), prob.tau, phi, prev)
+    xn, _, sn = go.gta_correction_new(*args, maxit=200, tol=1e-10)
+    xo, _, so = go.gta_correction(*args, maxit=200, tol=1e-10)
+    assert np.abs(xn - xo).max() <= 1e-9 * np.abs(xo).max()
+    assert sn < so

@@ -15,6 +15,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libumt103.so")
 
 UMT_FP64, UMT_FP32, UMT_MIXED = 0, 1, 2
+UMT_GTA_TSA, UMT_GTA_ZONE = 1, 2
 (UMT_OK, UMT_ERR_ARG, UMT_ERR_STATE, UMT_ERR_CUDA, UMT_ERR_CYCLE, UMT_ERR_TIMEOUT, UMT_ERR_BOUNDS,
  UMT_ERR_NOMEM, UMT_ERR_NOTCONV) = (0, -1, -2, -3, -4, -5, -6, -7, -8)
 
@@ -95,7 +96,7 @@ def load():
                   "umt103_schedule_info", "umt103_get_schedule", "umt103_get_geometry",
                   "umt103_last_timing", "umt103_launches_per_sweep", "umt103_select_device",
                   "umt103_set_group_tile", "umt103_tally_precision", "umt103_set_sweep_mode",
-                  "umt103_set_gta", "umt103_tally_noalloc", "umt103_context_create",
+                  "umt103_set_gta", "umt103_set_gta_solver", "umt103_tally_noalloc", "umt103_context_create",
                   "umt103_init_rz", "umt103_sweep_rz", "umt103_get_geometry_rz",
                   "umt103_context_select", "umt103_context_current", "umt103_context_destroy",
                   "umt103_batch_sweep", "umt103_psib_rows", "umt103_hold_item",
@@ -124,7 +125,7 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_get_schedule", "umt103_get_geometry", "umt103_last_sweep_ms",
             "umt103_error_string", "umt103_last_timing", "umt103_launches_per_sweep",
             "umt103_select_device", "umt103_set_group_tile", "umt103_tally_precision",
-            "umt103_set_sweep_mode", "umt103_set_gta", "umt103_tally_noalloc",
+            "umt103_set_sweep_mode", "umt103_set_gta", "umt103_set_gta_solver", "umt103_tally_noalloc",
             "umt103_context_create", "umt103_context_select", "umt103_context_current",
             "umt103_context_destroy", "umt103_batch_sweep", "umt103_init_rz", "umt103_sweep_rz",
             "umt103_get_geometry_rz", "umt103_psib_rows", "umt103_hold_item",
@@ -380,6 +381,11 @@ class Library:
     def set_gta(self, max_krylov=10, tol=1e-4, spectrum=0):
         self.lib.umt103_set_gta.argtypes = [C.c_int, C.c_double, C.c_int]
         check(self.lib.umt103_set_gta(int(max_krylov), float(tol), int(spectrum)))
+
+    def set_gta_solver(self, solver):
+        """umt103_set_gta_solver: UMT_GTA_TSA (grey + stretched-TSA sweeps) or
+        UMT_GTA_ZONE (grey sweep + per-zone direct solve)."""
+        check(self.lib.umt103_set_gta_solver(int(solver)))
 
     def phi_device(self):
         """umt103_phi_device: (device address, element count) of PhiTotal."""

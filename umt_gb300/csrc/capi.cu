@@ -72,7 +72,7 @@ static void free_ctx(Ctx &c) {
   dfree(c.Sigt); dfree(c.SigS); dfree(c.Sigt32); dfree(c.STotal); dfree(c.STotal32); dfree(c.Phi);
   dfree(c.PhiPrev); dfree(c.qExt); dfree(c.red); dfree(c.siDelta); dfree(c.siDeltaPrev); dfree(c.siKeep);
   dfree(c.siState); dfree(c.siRef); dfree(c.psiB32h); dfree(c.mixX); dfree(c.mixR); dfree(c.mixD);
-  dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS); dfree(c.gtaZ);
+  dfree(c.gtaChi); dfree(c.gtaVec); dfree(c.gtaSigS); dfree(c.gtaZ); dfree(c.gtaTT); dfree(c.gtaLU);
   for (int i = 0; i < 2; ++i) { dfree(c.psi64[i]); dfree(c.psi32[i]); }
   dfree(c.psiB64); dfree(c.psiB32); dfree(c.status); dfree(c.scratch); dfree(c.stage64); dfree(c.bFace);
   dfree(c.psibOut); dfree(c.phiOut);
@@ -874,6 +874,15 @@ int umt103_set_gta(int max_krylov, double tol, int spectrum) {
   return 0;
 }
 
+int umt103_set_gta_solver(int solver) {
+  Ctx &c = cur();
+  if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
+  if (solver != UMT_GTA_TSA && solver != UMT_GTA_ZONE)
+    return set_error(UMT_ERR_ARG, "GTA solver must be UMT_GTA_TSA (1) or UMT_GTA_ZONE (2)");
+  c.gtaSolver = solver;
+  return 0;
+}
+
 int umt103_set_sweep_mode(int mode) {
   Ctx &c = cur();
   if (!c.ready) return set_error(UMT_ERR_STATE, "umt103_init not called");
@@ -942,6 +951,9 @@ int umt103_get_geometry(double *A_fp, double *A_ez, double *Volume) {
 // iteration stops when the zone-averaged correction changes by less than
 // tol relative to the zone energy plus correction (pointwise and L2), or
 // after max_krylov iterations.  Then phi_g += chi_g x (rt/addGreyCorrections.F90).
+// With UMT_GTA_ZONE the operator is GreySweepNEW's (rt/GreySweep.F90:12-47,
+// rt/GTASolver.F90:158-174): one grey sweep, then the per-zone direct solve
+// (gta_op_zone), in place of the grey and stretched sweeps.
 // Vectors (FP64, device) in c.gtaVec: 0 x (GreyCorrection), 1 r, 3 d, 4 Ad,
 // 5 As, 7 R (grey source).  apply=false leaves PhiTotal unchanged.
 static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps, bool apply = true) {
@@ -949,10 +961,15 @@ static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps, bool apply 
   double *V = c.gtaVec;
   double *x = V, *r = V + (size_t)n, *d = V + 3 * (size_t)n, *Ad = V + 4 * (size_t)n, *As = V + 5 * (size_t)n;
   const double small = 1.0e-150;                  // adqtSmall, mods/constant_mod.F90:51
+  const bool zoneSolve = c.gtaSolver == UMT_GTA_ZONE;
+  auto op = [&](const double *P, double *out, bool withSource) -> int {
+    *greySweeps += zoneSolve ? 1 : 2;
+    return zoneSolve ? gta_op_zone(c, P, out, withSource) : gta_op(c, P, out, withSource);
+  };
   TRY(gta_prepare(c));
+  if (zoneSolve) TRY(gta_prepare_zone(c));
   UMT_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 8, c.stream));
-  TRY(gta_op(c, nullptr, r, true));               // CGResidual: M with the grey source, from zero
-  *greySweeps += 2;
+  TRY(op(nullptr, r, true));                      // CGResidual: M with the grey source, from zero
   UMT_CUDA(cudaMemcpyAsync(d, r, (size_t)n * 8, cudaMemcpyDeviceToDevice, c.stream));
   double h[2];
   TRY(gta_sdot2(c, r, nullptr, nullptr, nullptr, h));
@@ -964,16 +981,14 @@ static int gta_solve(Ctx &c, int maxit, double tol, int *greySweeps, bool apply 
       break;
     }
     nGrey += 2;
-    TRY(gta_op(c, d, Ad, false));                 // Ad = d - M d
-    *greySweeps += 2;
+    TRY(op(d, Ad, false));                        // Ad = d - M d
     TRY(gta_axpbypcz(c, n, 1.0, d, -1.0, Ad, 0.0, nullptr));
     TRY(gta_sdot2(c, Ad, nullptr, nullptr, nullptr, h));
     const double dAd = h[0];
     if (std::fabs(dAd) < small) break;
     const double alpha = rrOld / dAd;
     TRY(gta_axpbypcz(c, n, -alpha, Ad, 1.0, r, 0.0, nullptr));          // r -= alpha Ad
-    TRY(gta_op(c, r, As, false));                 // As = r - M r
-    *greySweeps += 2;
+    TRY(op(r, As, false));                        // As = r - M r
     TRY(gta_axpbypcz(c, n, 1.0, r, -1.0, As, 0.0, nullptr));
     TRY(gta_sdot2(c, As, r, As, As, h));
     const double omegaNum = h[0], omegaDen = h[1];
@@ -1006,6 +1021,10 @@ static int gta_alloc(Ctx &c) {
   if (!c.gtaSigS) TRY(dalloc(&c.gtaSigS, c.nz));
   if (!c.gtaZ) TRY(dalloc(&c.gtaZ, 5 * (size_t)c.nz));
   if (!c.red) TRY(dalloc(&c.red, 16));
+  if (c.gtaSolver == UMT_GTA_ZONE && !c.gtaTT) {
+    TRY(dalloc(&c.gtaTT, 8 * (size_t)c.nc));
+    TRY(dalloc(&c.gtaLU, 8 * (size_t)c.nc));
+  }
   return 0;
 }
 

@@ -366,6 +366,175 @@ __global__ void k_sdot2(int nc, const int *cToZone, const double *greySigs, cons
   block_reduce_add<2>(v, out2);
 }
 
+// ---------------------------------------------------------------------------
+// The newer grey solver (Size%useNewGTASolver; driver option gta_kernel = 2):
+// the stretched-TSA sweep is replaced by a direct solve, per zone, of the
+// zone-local scattering.
+//
+// k_gta_tt restates snac/InitSweepGreyUCBxyz.F90:10-253: for every grey
+// direction, the matrix Pvv[c][cc] = d psi(c) / d TsaSource(cc) of the zone's
+// corner solve (volume source, EZ closure, corner order by least need) is
+// formed and TT = sum_a w_a Pvv is kept; then A = I - TT diag(wtiso sigma_s)
+// is factored in place as snac/UpdateScalarIntensity.F90's
+// ScalarIntensityDecompose does (unit lower L, upper U, the same loop order).
+// Storage per corner row: tt[(c0+c)*8 + cc] = TT(cc, c0+c) of the reference,
+// lu[(c0+row)*8 + col] = its factored TT(col, c0+row).
+//
+// The reference's sweep also accumulates PhiInc, the part of the scalar flux
+// carried in by upwind flux (SweepGreyUCBxyzKernelNew's pInc).  The sweep is
+// linear, so PhiInc = tPhi - TT TsaSource exactly: k_gta_zone_solve takes
+// the library's ordinary grey sweep and subtracts the zone-local part.  With
+// TsaSource = wtiso (sigma_s P + [R]), the right-hand side of either call of
+// ScalarIntensityDecompose (PhiInc, plus TT wtiso R when the source is on)
+// is tPhi - TT wtiso sigma_s P.
+// ---------------------------------------------------------------------------
+__global__ void k_gta_tt(int nz, int nc, int A, const int *numCorner, const int *cOffSet, const int *nCFaces,
+                         const int *cEZ, const double *Volume, const double *afp, const double *aez,
+                         const double *weight, const double *greySigt, const double *greySigs, double *tt,
+                         double *lu) {
+  for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const int c0 = cOffSet[z], nC = numCorner[z];
+    const double sig = greySigt[z];
+    double T[8][8];                                // T[cc][c] = TT(cc, c0+c)
+    for (int a = 0; a < 8; ++a)
+      for (int b = 0; b < 8; ++b) T[a][b] = 0.0;
+    for (int ang = 0; ang < A; ++ang) {
+      const double w = weight[ang];
+      double P[8][8];                              // P[col][row] = Pvv(col, row)
+      double denom[8], coefpsi[8][3];
+      int need[8], nxez[8], ezx[8][3];
+      for (int a = 0; a < 8; ++a) {
+        need[a] = 0; nxez[a] = 0; denom[a] = 0.0;
+        for (int b = 0; b < 8; ++b) P[a][b] = 0.0;
+      }
+      for (int c = 0; c < nC; ++c) P[c][c] = Volume[c0 + c];
+      for (int c = 0; c < nC; ++c) {
+        const size_t cc = (size_t)ang * nc + c0 + c;
+        const double sigv = Volume[c0 + c] * sig;
+        denom[c] = sigv;
+        const int ncf = nCFaces[c0 + c];
+        double af[3];
+        for (int f = 0; f < ncf; ++f) {
+          af[f] = afp[cc * UMT_MAXCF + f];
+          if (af[f] > 0.0) denom[c] += af[f];
+        }
+        for (int f = 0; f < ncf; ++f) {
+          const double ae = aez[cc * UMT_MAXCF + f];
+          const int cez = cEZ[(size_t)(c0 + c) * UMT_MAXCF + f];
+          if (cez > c) {
+            if (ae > 0.0) {
+              need[cez] += 1;
+              ezx[c][nxez[c]] = cez; coefpsi[c][nxez[c]] = ae; nxez[c] += 1;
+            } else if (ae < 0.0) {
+              need[c] += 1;
+              ezx[cez][nxez[cez]] = c; coefpsi[cez][nxez[cez]] = -ae; nxez[cez] += 1;
+            }
+          }
+          if (ae > 0.0) {
+            denom[c] += ae;
+            double area_opp = 0.0;
+            if (ncf == 3) {
+              const int ifp = (f + 1) % ncf;
+              if (af[ifp] < 0.0) area_opp = -af[ifp];
+            } else {
+              int ifp = f;
+              for (int k = 0; k < ncf - 2; ++k) {
+                ifp = (ifp + 1) % ncf;
+                if (af[ifp] < 0.0) area_opp -= af[ifp];
+              }
+            }
+            double B1, B2;
+            if (area_opp > 0.0) {
+              const double sigv2 = sigv * sigv;
+              const double gnum = ae * ae * (1.82 * sigv2 + ae * (4.0 * sigv + 3.0 * ae));
+              const double gtau = gnum / (gnum + 4.0 * sigv2 * sigv2 + ae * sigv * (6.0 * sigv2 + 2.0 * ae * (2.0 * sigv + ae)));
+              const double B0 = 0.5 * ae * (1.0 - gtau);
+              B1 = (B0 - gtau * sigv) / sig;
+              B2 = B0 / sig;
+            } else {
+              B1 = 0.5 * ae / sig;
+              B2 = 0.5 * ae / sig;
+            }
+            P[c][c] += B1;
+            P[cez][c] -= B2;
+            P[c][cez] -= B1;
+            P[cez][cez] += B2;
+          }
+        }
+      }
+      for (int i = 0; i < nC; ++i) {
+        int c = 0;                                 // minloc: first index of the least need
+        for (int k = 1; k < nC; ++k) if (need[k] < need[c]) c = k;
+        const double dInv = 1.0 / denom[c];
+        for (int c1 = 0; c1 < nC; ++c1) P[c1][c] *= dInv;
+        for (int f = 0; f < nxez[c]; ++f) {
+          const int cez = ezx[c][f];
+          const double coef = coefpsi[c][f];
+          need[cez] -= 1;
+          for (int c1 = 0; c1 < nC; ++c1) P[c1][cez] += coef * P[c1][c];
+        }
+        need[c] = 99;
+      }
+      for (int c1 = 0; c1 < nC; ++c1)
+        for (int c = 0; c < nC; ++c) T[c][c1] += w * P[c][c1];
+    }
+    for (int c = 0; c < nC; ++c)
+      for (int cc = 0; cc < 8; ++cc) tt[(size_t)(c0 + c) * 8 + cc] = cc < nC ? T[cc][c] : 0.0;
+    // A = I - TT diag(wtiso sigma_s), factored in place
+    const double ws = WTISO * greySigs[z];
+    for (int cc = 0; cc < nC; ++cc)
+      for (int c = 0; c < nC; ++c) T[cc][c] = -ws * T[cc][c];
+    for (int c = 0; c < nC; ++c) T[c][c] = 1.0 + T[c][c];
+    for (int i = 0; i < nC; ++i) {
+      double t = 0.0;
+      for (int k = 0; k < i; ++k) t += T[k][i] * T[i][k];
+      T[i][i] -= t;
+      const double diagInv = 1.0 / T[i][i];
+      for (int j = i + 1; j < nC; ++j) {
+        double t2 = 0.0, v = 0.0;
+        for (int k = 0; k < i; ++k) {
+          t2 += T[k][i] * T[j][k];
+          v += T[k][j] * T[i][k];
+        }
+        T[j][i] -= t2;
+        T[i][j] = diagInv * (T[i][j] - v);
+      }
+    }
+    for (int row = 0; row < nC; ++row)
+      for (int col = 0; col < 8; ++col) lu[(size_t)(c0 + row) * 8 + col] = col < nC ? T[col][row] : 0.0;
+  }
+}
+
+// out = A^-1 (tPhi - TT wtiso sigma_s P) per zone (ScalarIntensitySolve:
+// L y = S, then U x = y); P may be null (zero).
+__global__ void k_gta_zone_solve(int nz, const int *numCorner, const int *cOffSet, const double *greySigs,
+                                 const double *tt, const double *lu, const double *tPhi, const double *P,
+                                 double *out) {
+  for (int z = blockIdx.x * blockDim.x + threadIdx.x; z < nz; z += gridDim.x * blockDim.x) {
+    const int c0 = cOffSet[z], nC = numCorner[z];
+    const double ws = WTISO * greySigs[z];
+    double x[8];
+    for (int c = 0; c < nC; ++c) {
+      double r = tPhi[c0 + c];
+      if (P)
+        for (int cc = 0; cc < nC; ++cc) r -= tt[(size_t)(c0 + c) * 8 + cc] * ws * P[c0 + cc];
+      x[c] = r;
+    }
+    for (int j = 1; j < nC; ++j) {
+      double t = 0.0;
+      for (int i = 0; i < j; ++i) t -= lu[(size_t)(c0 + j) * 8 + i] * x[i];
+      x[j] += t;
+    }
+    x[nC - 1] /= lu[(size_t)(c0 + nC - 1) * 8 + nC - 1];
+    for (int k = nC - 2; k >= 0; --k) {
+      double t = 0.0;
+      for (int i = k + 1; i < nC; ++i) t += x[i] * lu[(size_t)(c0 + k) * 8 + i];
+      x[k] = (x[k] - t) / lu[(size_t)(c0 + k) * 8 + k];
+    }
+    for (int c = 0; c < nC; ++c) out[c0 + c] = x[c];
+  }
+}
+
 // Grey problem of this iterate: spectrum and grey opacities (k_gta_spectrum),
 // the stretched-TSA opacities, the grey source R = sum_g sigma_s,g (phi_g -
 // phi_g_prev) in slot 7 of the vectors, the zone radiation energy.
@@ -405,6 +574,33 @@ int gta_op(Ctx &c, const double *P, double *out, bool withSource) {
   TRY_SI(launch_sweep_once(q, 0, true));
   UMT_CUDA(cudaMemcpyAsync(q.Sigt, Z + c.nz, c.nz * 8, cudaMemcpyDeviceToDevice, q.stream));
   k_axpbypcz<<<152 * 4, 256, 0, q.stream>>>(c.nc, 1.0, q.Phi, 1.0, out, 0.0, nullptr);
+  UMT_CUDA(cudaGetLastError());
+  UMT_CUDA(cudaStreamSynchronize(q.stream));
+  return 0;
+}
+
+// The newer solver's transfer matrices and their factors for this iterate's
+// grey opacities (after gta_prepare).
+int gta_prepare_zone(Ctx &c) {
+  Ctx &q = *c.gta;
+  k_gta_tt<<<(c.nz + 63) / 64, 64, 0, c.stream>>>(c.nz, c.nc, q.A, c.numCorner, c.cOffSet, c.nCFaces, c.cEZ,
+                                                  c.Volume, q.afp64, q.aez64, q.weight, q.Sigt, c.gtaSigS,
+                                                  c.gtaTT, c.gtaLU);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// out = M P of the newer solver (rt/GreySweep.F90 GreySweepNEW): one grey S2
+// sweep of wtiso (sigma_s P + [R]), then the per-zone solve.  One grey sweep.
+int gta_op_zone(Ctx &c, const double *P, double *out, bool withSource) {
+  Ctx &q = *c.gta;
+  k_gta_source<<<152 * 4, 256, 0, c.stream>>>(c.nc, c.cToZone, c.gtaSigS, P, c.gtaVec + 7 * (size_t)c.nc,
+                                              withSource ? 1.0 : 0.0, q.STotal);
+  UMT_CUDA(cudaGetLastError());
+  UMT_CUDA(cudaStreamSynchronize(c.stream));
+  TRY_SI(launch_sweep_once(q, 0, true));
+  k_gta_zone_solve<<<(c.nz + 127) / 128, 128, 0, q.stream>>>(c.nz, c.numCorner, c.cOffSet, c.gtaSigS, c.gtaTT,
+                                                              c.gtaLU, q.Phi, P, out);
   UMT_CUDA(cudaGetLastError());
   UMT_CUDA(cudaStreamSynchronize(q.stream));
   return 0;

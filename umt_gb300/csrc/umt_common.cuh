@@ -158,6 +158,8 @@ struct Ctx {
   int gtaMaxKrylov = 10;                        // BiCGStab iterations per correction (2 grey sweeps each)
   double gtaTol = 1.0e-4;                       // BiCGStab relative residual
   int gtaSpectrum = 0;                          // correction spectrum (see k_gta_spectrum)
+  int gtaSolver = 1;                            // 1 UMT_GTA_TSA, 2 UMT_GTA_ZONE (umt103_set_gta_solver)
+  double *gtaTT = nullptr, *gtaLU = nullptr;    // [nc][8] zone transfer matrices, factored A (UMT_GTA_ZONE)
 };
 
 extern Ctx *g_cur;
@@ -208,6 +210,8 @@ int launch_inner_update(Ctx &c, const double *R, double *D, double *delta, doubl
 // grey transport acceleration (si.cu)
 int gta_prepare(Ctx &c);
 int gta_op(Ctx &c, const double *P, double *out, bool withSource);
+int gta_prepare_zone(Ctx &c);
+int gta_op_zone(Ctx &c, const double *P, double *out, bool withSource);
 int gta_sdot2(Ctx &c, const double *x, const double *y, const double *u, const double *w, double *h2);
 int gta_converge(Ctx &c, const double *x, double *rel);
 int gta_axpbypcz(Ctx &c, int n, double a, const double *x, double b, double *y, double cc, const double *z);
