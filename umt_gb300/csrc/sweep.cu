@@ -37,9 +37,26 @@ struct SweepP {
 
 constexpr int SWEEP_NT = 128;
 
+// Per (direction, zone) the team first classifies the zone's corner faces
+// once, into integer masks (incoming FP faces, exiting boundary faces, EZ
+// faces that carry flux, and of those the ones whose opposite FP face is
+// incoming), so that the per-group loop runs no floating-point comparison of
+// geometry.  With PRE (four or more lanes per zone) it also forms, per EZ
+// face that carries flux, the coefficients of the closure as polynomials in
+// the group's total opacity s = sigma_t:
+//   gnum   = aez^2 (1.82 s^2 V^2 + 4 aez s V + 3 aez^2) = (k0 s + k1) s + k2
+//   gden   = V (4 s^3 V^3 + 6 aez s^2 V^2 + 4 aez^2 s V + 2 aez^3)
+//          = ((k3 s + k4) s + k5) s + k6,                       k7 = aez/2
+//   sez    = (V gnum (s psi_opp - Qc) + k7 gden (Qc - Qz)) / (gnum + gden s)
+// (SweepUCBxyz.F90:219-243 with the products over the corner and face
+// gathered), so a group pays 5 FMAs for both polynomials instead of forming
+// them from the products again.  GB300's FP64 pipe executes two lanes per
+// clock per SM, and this kernel's time is its FP64 instruction count.
 template <typename T, int GT>
 __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
   constexpr int TEAMS = SWEEP_NT / GT;
+  constexpr bool PRE = GT >= 4;
+  constexpr int KT = PRE ? TEAMS : 1;
   __shared__ T s_src[UMT_MAXCORNER][SWEEP_NT];
   __shared__ T s_Q[UMT_MAXCORNER][SWEEP_NT];
   __shared__ T s_psi[UMT_MAXCORNER][SWEEP_NT];
@@ -47,9 +64,12 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
   __shared__ T s_aez[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
   __shared__ T s_sum[TEAMS][UMT_MAXCORNER];
   __shared__ T s_vol[TEAMS][UMT_MAXCORNER];
+  __shared__ T s_k[KT][UMT_MAXCORNER][UMT_MAXCF][8];
   __shared__ int s_cfp[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
   __shared__ int8_t s_cez[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
-  __shared__ int8_t s_ncf[TEAMS][UMT_MAXCORNER];
+  __shared__ uint8_t s_in[TEAMS][UMT_MAXCORNER], s_ex[TEAMS][UMT_MAXCORNER];
+  __shared__ uint8_t s_ez[TEAMS][UMT_MAXCORNER], s_opp[TEAMS][UMT_MAXCORNER];
+  __shared__ int s_anyNoOpp[TEAMS];
 
   const int tid = threadIdx.x, team = tid / GT, lane = tid % GT;
   const int k = blockIdx.x * TEAMS + team;
@@ -65,34 +85,69 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
   const uint32_t ord = p.order[it];
   const size_t abase = (size_t)a * p.nc;
 
+  if (lane == 0) s_anyNoOpp[team] = 0;
+  __syncwarp(teammask);
   for (int c = lane; c < nCorner; c += GT) {
     const int cc = c0 + c;
     const int ncf = p.nCFaces[cc];
-    s_ncf[team][c] = (int8_t)ncf;
-    s_vol[team][c] = (T)p.Volume[cc];
-    T sum = T(0);
+    const T vol = (T)p.Volume[cc];
+    s_vol[team][c] = vol;
+    T sum = T(0), af[UMT_MAXCF];
+    uint32_t in = 0, ex = 0, ez = 0, opp = 0;
 #pragma unroll
     for (int cf = 0; cf < UMT_MAXCF; ++cf) {
       const T v = p.afp[(abase + cc) * UMT_MAXCF + cf];
+      const int cfp = p.cFP[cc * UMT_MAXCF + cf];
+      af[cf] = v;
       s_afp[team][c][cf] = v;
-      s_cfp[team][c][cf] = p.cFP[cc * UMT_MAXCF + cf];
-      if (cf < ncf && v > T(0)) sum = sum + v;
+      s_cfp[team][c][cf] = cfp;
+      if (cf < ncf && v > T(0)) {
+        sum = sum + v;
+        if (cfp >= p.nc) ex |= 1u << cf;
+      }
+      if (cf < ncf && v < T(0)) in |= 1u << cf;
     }
 #pragma unroll
     for (int cf = 0; cf < UMT_MAXCF; ++cf) {
       const T v = p.aez[(abase + cc) * UMT_MAXCF + cf];
       s_aez[team][c][cf] = v;
       s_cez[team][c][cf] = (int8_t)p.cEZ[cc * UMT_MAXCF + cf];
-      if (cf < ncf && v > T(0)) sum = sum + v;
+      if (cf < ncf && v > T(0)) {
+        sum = sum + v;
+        ez |= 1u << cf;
+        const bool o = ncf == 3 && af[(cf + 1) % 3] < T(0);
+        if (o) opp |= 1u << cf;
+        else s_anyNoOpp[team] = 1;
+        if constexpr (PRE) {
+          if (o) {
+            const T aez2 = v * v, V2 = vol * vol;
+            T *kc = s_k[team][c][cf];
+            kc[0] = T(1.82) * aez2 * V2;
+            kc[1] = T(4) * aez2 * v * vol;
+            kc[2] = T(3) * aez2 * aez2;
+            kc[3] = T(4) * V2 * V2;
+            kc[4] = T(6) * v * V2 * vol;
+            kc[5] = T(4) * aez2 * V2;
+            kc[6] = T(2) * aez2 * v * vol;
+            kc[7] = T(0.5) * v;
+          }
+        }
+      }
     }
     s_sum[team][c] = sum;
+    s_in[team][c] = (uint8_t)in;
+    s_ex[team][c] = (uint8_t)ex;
+    s_ez[team][c] = (uint8_t)ez;
+    s_opp[team][c] = (uint8_t)opp;
   }
   __syncwarp(teammask);
 
   const T fouralpha = T(1.82);
   const T *sigz = p.Sigt + (size_t)z * p.G;
+  const bool anyNoOpp = s_anyNoOpp[team] != 0;
   for (int g = lane; g < p.G; g += GT) {
     const T sig = sigz[g];
+    const T sigInv = anyNoOpp ? T(1) / sig : T(0);
     for (int c = 0; c < nCorner; ++c) {
       const size_t e = (size_t)(c0 + c) * p.G + g;
       const T st = p.STotal ? p.STotal[e] : T(0);
@@ -101,47 +156,49 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
       s_src[c][tid] = s_vol[team][c] * q;
     }
     for (int c = 0; c < nCorner; ++c) {
-      const int ncf = s_ncf[team][c];
+      const uint32_t in = s_in[team][c], ezm = s_ez[team][c], opp = s_opp[team][c];
       T psifp[UMT_MAXCF];
       T srcc = s_src[c][tid];
 #pragma unroll
       for (int cf = 0; cf < UMT_MAXCF; ++cf) {
         psifp[cf] = T(0);
-        const T af = s_afp[team][c][cf];
-        if (cf < ncf && af < T(0)) {
+        if ((in >> cf) & 1u) {
           const int cfp = s_cfp[team][c][cf];
           const T pu = (cfp < p.nc) ? p.psi_new[(abase + cfp) * p.G + g]
                                     : p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g];
           psifp[cf] = pu;
-          srcc = srcc - af * pu;
+          srcc = srcc - s_afp[team][c][cf] * pu;
         }
       }
       s_src[c][tid] = srcc;
       const T Qc = s_Q[c][tid];
 #pragma unroll
       for (int cf = 0; cf < UMT_MAXCF; ++cf) {
-        const T aez = s_aez[team][c][cf];
-        if (cf < ncf && aez > T(0)) {
+        if ((ezm >> cf) & 1u) {
           const int cez = s_cez[team][c][cf];
-          T area_opp = T(0), psi_opp = T(0);
-          if (ncf == 3) {
-            const int ifp = (cf + 1) % 3;
-            const T afo = s_afp[team][c][ifp];
-            if (afo < T(0)) { psi_opp = psifp[ifp]; area_opp = -afo; }
-          }
           const T Qz = s_Q[cez][tid];
           T sez;
-          if (area_opp > T(0)) {
-            const T aez2 = aez * aez;
+          if ((opp >> cf) & 1u) {
+            const T psi_opp = psifp[(cf + 1) % 3];
             const T vol = s_vol[team][c];
-            const T sigv = sig * vol;
-            const T sigv2 = sigv * sigv;
-            const T gnum = aez2 * (fouralpha * sigv2 + aez * (T(4) * sigv + T(3) * aez));
-            const T gden = vol * (T(4) * sigv * sigv2 + aez * (T(6) * sigv2 + T(2) * aez * (T(2) * sigv + aez)));
-            sez = (vol * gnum * (sig * psi_opp - Qc) + T(0.5) * aez * gden * (Qc - Qz)) / (gnum + gden * sig);
+            T gnum, gden, half_aez;
+            if constexpr (PRE) {
+              const T *kc = s_k[team][c][cf];
+              gnum = (kc[0] * sig + kc[1]) * sig + kc[2];
+              gden = ((kc[3] * sig + kc[4]) * sig + kc[5]) * sig + kc[6];
+              half_aez = kc[7];
+            } else {
+              const T aez = s_aez[team][c][cf];
+              const T aez2 = aez * aez;
+              const T sigv = sig * vol;
+              const T sigv2 = sigv * sigv;
+              gnum = aez2 * (fouralpha * sigv2 + aez * (T(4) * sigv + T(3) * aez));
+              gden = vol * (T(4) * sigv * sigv2 + aez * (T(6) * sigv2 + T(2) * aez * (T(2) * sigv + aez)));
+              half_aez = T(0.5) * aez;
+            }
+            sez = (vol * gnum * (sig * psi_opp - Qc) + half_aez * gden * (Qc - Qz)) / (gnum + gden * sig);
           } else {
-            const T sigInv = T(1) / sig;
-            sez = T(0.5) * aez * sigInv * (Qc - Qz);
+            sez = T(0.5) * s_aez[team][c][cf] * sigInv * (Qc - Qz);
           }
           s_src[c][tid] = s_src[c][tid] + sez;
           s_src[cez][tid] = s_src[cez][tid] - sez;
@@ -155,13 +212,12 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
         const T v = s_src[c][tid] / (s_sum[team][c] + sig * s_vol[team][c]);
         out[(size_t)(c0 + c) * p.G + g] = v;
         s_psi[c][tid] = v;
-        const int ncf = s_ncf[team][c];
+        const uint32_t ezm = s_ez[team][c];
 #pragma unroll
         for (int cf = 0; cf < UMT_MAXCF; ++cf) {
-          const T aez = s_aez[team][c][cf];
-          if (cf < ncf && aez > T(0)) {
+          if ((ezm >> cf) & 1u) {
             const int cez = s_cez[team][c][cf];
-            s_src[cez][tid] = s_src[cez][tid] + aez * v;
+            s_src[cez][tid] = s_src[cez][tid] + s_aez[team][c][cf] * v;
           }
         }
       }
@@ -169,12 +225,11 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
       // direct solve with the previous iterate of this zone (SweepUCBxyz.F90:283-297)
       for (int c = 0; c < nCorner; ++c) {
         const T old = out[(size_t)(c0 + c) * p.G + g];
-        const int ncf = s_ncf[team][c];
-        for (int cf = 0; cf < ncf; ++cf) {
-          const T aez = s_aez[team][c][cf];
-          if (aez > T(0)) {
+        const uint32_t ezm = s_ez[team][c];
+        for (int cf = 0; cf < UMT_MAXCF; ++cf) {
+          if ((ezm >> cf) & 1u) {
             const int cez = s_cez[team][c][cf];
-            s_src[cez][tid] = s_src[cez][tid] + aez * old;
+            s_src[cez][tid] = s_src[cez][tid] + s_aez[team][c][cf] * old;
           }
         }
       }
@@ -186,12 +241,12 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
     }
     // exiting boundary fluxes
     for (int c = 0; c < nCorner; ++c) {
-      const int ncf = s_ncf[team][c];
-      for (int cf = 0; cf < ncf; ++cf) {
-        const int cfp = s_cfp[team][c][cf];
-        if (cfp >= p.nc && s_afp[team][c][cf] > T(0))
+      const uint32_t ex = s_ex[team][c];
+      for (int cf = 0; cf < UMT_MAXCF; ++cf)
+        if ((ex >> cf) & 1u) {
+          const int cfp = s_cfp[team][c][cf];
           p.psiB[((size_t)a * p.nb + (cfp - p.nc)) * p.G + g] = s_psi[c][tid];
-      }
+        }
     }
   }
 }
