@@ -42,7 +42,7 @@
 
 namespace umt {
 
-constexpr int P32_NT = 128;
+constexpr int P32_NT = 64;             // two warps: a block's slot frees when its 8 items are done
 constexpr int P32_MAXCHUNK = 48;        // 16-byte units: 8 + 8*(8+24+24+24) + 4*24 bytes
 
 struct ProgP {
@@ -84,7 +84,7 @@ __host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 
 // WT: also write the exiting rows, in FP64, to *p.psibOut (the variant used
 // by calls that return PsiB to the host; resident sweeps run the other).
 template <int GT, int GPL, bool WT>
-__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 7 : 6) k_sweep32p(ProgP p, int off, int nItems) {
+__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32p(ProgP p, int off, int nItems) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
   constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
   constexpr int G = GT * GPL;
