@@ -508,7 +508,7 @@ def run_config4(args):
     if args.c4_max_batches:
         batches = batches[:args.c4_max_batches]
     tot_units, tot_balg = 0, 0.0
-    tb_ms = ts_ms = wb_ms = ws_ms = 0.0
+    tb_ms = ts_ms = wb_ms = ws_ms = tn_ms = 0.0
     per_batch = []
     with ClockSampler(0) as clk:
         for taken in batches:
@@ -542,6 +542,12 @@ def run_config4(args):
                 t0 = time.perf_counter()
                 batch_ms.append(lib.batch_sweep(ids, capi.UMT_FP32))
                 batch_wall.append((time.perf_counter() - t0) * 1e3)
+            # the same batch with every dependency stage of the problems of a group tile in one launch
+            lib.set_batch_mode(capi.UMT_BATCH_MERGED)
+            for _ in range(args.warmup):
+                lib.batch_sweep(ids, capi.UMT_FP32)
+            merged_ms = [lib.batch_sweep(ids, capi.UMT_FP32) for _ in range(args.steps)]
+            lib.set_batch_mode(capi.UMT_BATCH_GRAPHS)
             seq_ms, seq_wall = [], []
             for _ in range(args.steps):
                 tot = 0.0
@@ -557,10 +563,12 @@ def run_config4(args):
                 lib.context_destroy(cid)
             b, sq = statistics.median(batch_ms), statistics.median(seq_ms)
             wb, ws = statistics.median(batch_wall), statistics.median(seq_wall)
-            tb_ms += b; ts_ms += sq; wb_ms += wb; ws_ms += ws
+            nb = statistics.median(merged_ms)
+            tb_ms += b; ts_ms += sq; wb_ms += wb; ws_ms += ws; tn_ms += nb
             tot_units += units
             tot_balg += balg_units
-            per_batch.append({"problems": len(taken), "units": units, "batch_ms": b, "sequential_ms": sq,
+            per_batch.append({"problems": len(taken), "units": units, "batch_ms": b, "merged_stages_ms": nb,
+                              "sequential_ms": sq,
                               "batch_wall_ms": wb, "sequential_wall_ms": ws,
                               "draws": [list(d[:3]) for d in taken]})
     peak, src = peaks()
@@ -570,7 +578,8 @@ def run_config4(args):
             "warmup": args.warmup, "ms_per_step": tb_ms, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "batch of independent problems (tiles per axis U{%d..%d}, G in {4..64}, "
-                                   "32 or 128 directions; seed 4), one graph launch per sub-batch" % tuple(args.c4_tiles),
+                                   "32 or 128 directions; seed 4), one graph launch per sub-batch "
+                                   "(each problem's sweep graph nested)" % tuple(args.c4_tiles),
                        "problems": ndraws, "of_draws": len(draws), "sub_batches": len(batches),
                        "device_budget_gb": args.c4_budget, "units_per_step": tot_units,
                        "autotuned": not args.c4_no_tune, "l2": "inputs larger than L2"},
@@ -580,6 +589,9 @@ def run_config4(args):
                          "bytes_per_unit": tot_balg / tot_units},
             "sequential": {"value": ts_ms * 1e6 / tot_units, "unit": "ns", "ms_per_step": ts_ms,
                            "how": "the same contexts swept one after another (umt103_sweep_resident)"},
+            "merged_stages": {"value": tn_ms * 1e6 / tot_units, "unit": "ns", "ms_per_step": tn_ms,
+                              "how": "the same batch with every dependency stage of the problems that share a "
+                                     "group tile in one kernel launch (umt103_set_batch_mode(UMT_BATCH_MERGED))"},
             "wall_clock": {"batch_ms": wb_ms, "sequential_ms": ws_ms, "ratio": ws_ms / wb_ms,
                            "how": "host time of each whole call (launch, wait, status checks); the batch "
                                   "graph is instantiated once and replayed (kept by umt103_batch_sweep)"},

@@ -124,6 +124,18 @@ int umt103_context_destroy(int id);   /* id > 0; releases its buffers */
  */
 int umt103_batch_sweep(const int *ids, int n, int precision, double *ms);
 
+/* How umt103_batch_sweep builds its graph.  UMT_BATCH_GRAPHS (1, default):
+ * each context's own sweep graph as a child node, so every problem's stages
+ * advance at their own pace.  UMT_BATCH_MERGED (0): for FP32 contexts on the
+ * zone-program kernel, every dependency stage of all the problems that share
+ * a group tile is one kernel launch (problems of different tiles on parallel
+ * streams), with each context's conversions, cycle rows and tally around
+ * them; it holds those problems in lockstep and measured 5-22% slower; any
+ * other batch falls back to the nested form.  Results are the same in both. */
+#define UMT_BATCH_MERGED 0
+#define UMT_BATCH_GRAPHS 1
+int umt103_set_batch_mode(int mode);
+
 /*
  * Materials: sigt = total opacity including tau, Sigt(G,nzones) as
  * setTotalOpacity builds it (control/setTotalOpacity.F90:52); sigs =

@@ -161,12 +161,23 @@ def _config4_draws(n=12, seed=4):
     return out
 
 
+@pytest.mark.parametrize("mode", [capi.UMT_BATCH_MERGED, capi.UMT_BATCH_GRAPHS], ids=["merged", "graphs"])
 @pytest.mark.parametrize("specs", [[((2, 2, 1), 2, 4, 31), ((3, 2, 1), 4, 8, 32), ((2, 3, 2), 2, 16, 33)],
                                    _config4_draws()], ids=["three", "config4_draws"])
-def test_batch_of_contexts_matches_single_runs(umtlib, specs):
+def test_batch_of_contexts_matches_single_runs(umtlib, specs, mode):
     """Several problems of different size, group and direction counts resident
     in separate contexts, swept from one graph launch, give each problem's
-    single-context result."""
+    single-context result bit for bit: with every dependency stage of the
+    problems that share a group tile in one launch (merged), and with each
+    context's own sweep graph nested (graphs)."""
+    umtlib.set_batch_mode(mode)
+    try:
+        _batch_case(umtlib, specs)
+    finally:
+        umtlib.set_batch_mode(capi.UMT_BATCH_GRAPHS)
+
+
+def _batch_case(umtlib, specs):
     from umt_gb300.problems import synthetic_problem as sp
     probs = [sp(t, P, P, G, seed=s, time_dependent=True) for (t, P, G, s) in specs]
     single = []

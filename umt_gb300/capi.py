@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libumt103.so")
 
 UMT_FP64, UMT_FP32, UMT_MIXED = 0, 1, 2
 UMT_GTA_TSA, UMT_GTA_ZONE = 1, 2
+UMT_BATCH_MERGED, UMT_BATCH_GRAPHS = 0, 1
 (UMT_OK, UMT_ERR_ARG, UMT_ERR_STATE, UMT_ERR_CUDA, UMT_ERR_CYCLE, UMT_ERR_TIMEOUT, UMT_ERR_BOUNDS,
  UMT_ERR_NOMEM, UMT_ERR_NOTCONV) = (0, -1, -2, -3, -4, -5, -6, -7, -8)
 
@@ -104,7 +105,7 @@ def load():
                   "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect", "umt103_mlp_set_targets",
                   "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train", "umt103_autotune",
                   "umt103_autotune_contexts", "umt103_gta_correction", "umt103_phi_device",
-                  "umt103_set_external_source", "umt103_si_step", "umt103_si_change"):
+                  "umt103_set_external_source", "umt103_si_step", "umt103_si_change", "umt103_set_batch_mode"):
             getattr(_lib, n).restype = C.c_int
         _lib.umt103_mlp_finalize.restype = None
         _fp = C.POINTER(C.c_float)
@@ -133,7 +134,7 @@ EXPORTED = ["umt103_init", "umt103_finalize", "umt103_set_materials", "umt103_se
             "umt103_mlp_set_params", "umt103_mlp_forward", "umt103_mlp_gradient", "umt103_mlp_collect",
             "umt103_mlp_set_targets", "umt103_mlp_rows", "umt103_mlp_clear", "umt103_mlp_train",
             "umt103_autotune", "umt103_autotune_contexts", "umt103_gta_correction", "umt103_phi_device",
-            "umt103_set_external_source", "umt103_si_step", "umt103_si_change"]
+            "umt103_set_external_source", "umt103_si_step", "umt103_si_change", "umt103_set_batch_mode"]
 
 
 def check(rc):
@@ -363,6 +364,12 @@ class Library:
         ms = C.c_double(0.0)
         check(self.lib.umt103_batch_sweep(arr, len(ids), int(precision), C.byref(ms)))
         return ms.value
+
+    def set_batch_mode(self, mode):
+        """umt103_set_batch_mode: UMT_BATCH_MERGED (one launch per dependency
+        stage over the problems of a group tile) or UMT_BATCH_GRAPHS (each
+        context's sweep graph nested)."""
+        check(self.lib.umt103_set_batch_mode(int(mode)))
 
     def set_group_tile(self, lanes_per_zone, groups_per_lane):
         check(self.lib.umt103_set_group_tile(int(lanes_per_zone), int(groups_per_lane)))

@@ -149,7 +149,7 @@ int umt103_context_destroy(int id) {
 struct BatchGraph {
   std::vector<int> ids, curs;
   std::vector<unsigned long long> gens;
-  int precision = -1;
+  int precision = -1, mode = -1;
   cudaGraphExec_t exec = nullptr;
 };
 static std::vector<BatchGraph> g_batch;          // most recently used last
@@ -255,11 +255,84 @@ int umt103_autotune_contexts(const int *ids, int n, int reps) {
   return rc;
 }
 
+// Batch mode: UMT_BATCH_GRAPHS (default) nests each context's own sweep
+// graph, so every problem's chain of stages advances at its own pace;
+// UMT_BATCH_MERGED launches each dependency stage of all FP32 zone-program
+// problems that share a group tile as one kernel (k_sweep32pm), one stream
+// per tile, which holds those problems in lockstep, stage by stage (measured
+// 5-22% slower on the config-4 draws).  Contexts the merged form cannot take
+// (FP64, another FP32 kernel) make the batch use the nested graphs.
+static int g_batchMode = UMT_BATCH_GRAPHS;
+
+int umt103_set_batch_mode(int mode) {
+  if (mode != UMT_BATCH_MERGED && mode != UMT_BATCH_GRAPHS) return set_error(UMT_ERR_ARG, "batch mode must be 0 or 1");
+  g_batchMode = mode;
+  return 0;
+}
+
+static cudaStream_t g_bStream[9];
+static cudaEvent_t g_bEvent[9];
+
+// The merged batch graph: every context's FP32 conversions and cycle rows,
+// then per group tile a forked stream with one launch per dependency stage
+// over the tile's problems, then every context's cycle update and tally.
+// Returns 1 when a context cannot take part.
+static int capture_batch_merged(const std::vector<int> &ids, cudaGraph_t *out) {
+  std::map<std::pair<int, int>, std::vector<int>> cls;
+  for (int id : ids) {
+    const Ctx &c = *g_ctx[id];
+    if (c.sweepMode != 0 || c.progState != 1 || c.homog32 || c.wantExitsThrough || c.tileGT <= 0 ||
+        !sweep32p_supported(c.G, c.tileGT, c.tileGPL))
+      return 1;
+    cls[{c.tileGT, c.tileGPL}].push_back(id);
+  }
+  if (cls.size() > 8) return 1;
+  for (int k = 0; k < 9; ++k) {
+    if (!g_bStream[k]) UMT_CUDA(cudaStreamCreateWithFlags(&g_bStream[k], cudaStreamNonBlocking));
+    if (!g_bEvent[k]) UMT_CUDA(cudaEventCreateWithFlags(&g_bEvent[k], cudaEventDisableTiming));
+  }
+  cudaStream_t s0 = g_bStream[0];
+  std::vector<cudaStream_t> saved;
+  for (int id : ids) saved.push_back(g_ctx[id]->stream);
+  UMT_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  for (int id : ids) g_ctx[id]->stream = s0;
+  int rc = 0;
+  cudaError_t e = cudaSuccess;
+  for (size_t j = 0; j < ids.size() && !rc; ++j) rc = enqueue_sweep32_pre(*g_ctx[ids[j]], g_ctx[ids[j]]->cur32);
+  if (!rc) e = cudaEventRecord(g_bEvent[0], s0);
+  int k = 1;
+  for (auto &kv : cls) {
+    if (rc || e != cudaSuccess) break;
+    cudaStream_t sk = g_bStream[k];
+    std::vector<Ctx *> cs;
+    std::vector<int> curs;
+    for (int id : kv.second) { cs.push_back(g_ctx[id]); curs.push_back(g_ctx[id]->cur32); }
+    e = cudaStreamWaitEvent(sk, g_bEvent[0], 0);
+    if (e == cudaSuccess) rc = enqueue_batch_stages(cs, curs, kv.first.first, kv.first.second, sk);
+    if (!rc && e == cudaSuccess) e = cudaEventRecord(g_bEvent[k], sk);
+    if (!rc && e == cudaSuccess) e = cudaStreamWaitEvent(s0, g_bEvent[k], 0);
+    ++k;
+  }
+  for (size_t j = 0; j < ids.size() && !rc && e == cudaSuccess; ++j)
+    rc = enqueue_sweep32_post(*g_ctx[ids[j]], g_ctx[ids[j]]->cur32);
+  for (size_t j = 0; j < ids.size(); ++j) g_ctx[ids[j]]->stream = saved[j];
+  cudaGraph_t gr = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(s0, &gr);
+  if (rc || e != cudaSuccess || e2 != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    if (rc) return rc;
+    return set_error(UMT_ERR_CUDA, "batch capture: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+  }
+  *out = gr;
+  return 0;
+}
+
 int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
   if (!ids || n <= 0) return set_error(UMT_ERR_ARG, "empty batch");
   if (precision != UMT_FP64 && precision != UMT_FP32) return set_error(UMT_ERR_ARG, "precision");
   BatchGraph key;
   key.precision = precision;
+  key.mode = g_batchMode;
   for (int k = 0; k < n; ++k) {
     const int id = ids[k];
     if (id < 0 || id >= (int)g_ctx.size() || !g_ctx[id] || !g_ctx[id]->ready)
@@ -294,11 +367,23 @@ int umt103_batch_sweep(const int *ids, int n, int precision, double *ms) {
   cudaGraphExec_t exec = nullptr;
   for (size_t k = 0; k < g_batch.size(); ++k) {
     const BatchGraph &b = g_batch[k];
-    if (b.precision == key.precision && b.ids == key.ids && b.curs == key.curs && b.gens == key.gens) {
+    if (b.precision == key.precision && b.mode == key.mode && b.ids == key.ids && b.curs == key.curs &&
+        b.gens == key.gens) {
       key.exec = b.exec;
       g_batch.erase(g_batch.begin() + (long)k);
       exec = key.exec;
       break;
+    }
+  }
+  if (!exec && precision == UMT_FP32 && g_batchMode == UMT_BATCH_MERGED) {
+    cudaGraph_t merged = nullptr;
+    const int mrc = capture_batch_merged(key.ids, &merged);
+    if (mrc < 0) return mrc;
+    if (mrc == 0) {
+      const cudaError_t e = cudaGraphInstantiate(&exec, merged, 0);
+      cudaGraphDestroy(merged);
+      if (e != cudaSuccess) return set_error(UMT_ERR_CUDA, "batch graph: %s", cudaGetErrorString(e));
+      key.exec = exec;
     }
   }
   if (!exec) {

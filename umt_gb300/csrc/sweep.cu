@@ -441,6 +441,28 @@ static int enqueue_sweep(Ctx &c, int cur) {
 
 static int prepare_precision(Ctx &c, int precision);
 
+// The parts of a resident FP32 zone-program sweep around its stages, for a
+// batch whose stages are launched together (enqueue_batch_stages): before,
+// the FP32 copies of the cross sections and the source and the cycle list's
+// lagged rows; after, the cycle list's update and the tally.  On c.stream.
+int enqueue_sweep32_pre(Ctx &c, int cur) {
+  const size_t n = (size_t)c.nz * c.G;
+  k_to_float<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(n, c.Sigt, c.Sigt32);
+  const size_t m = (size_t)c.nc * c.G;
+  k_to_float<<<(int)std::min<size_t>((m + 255) / 256, 4096), 256, 0, c.stream>>>(m, c.STotal, c.STotal32);
+  UMT_CUDA(cudaGetLastError());
+  return enqueue_cycle_init(c, 1, cur);
+}
+
+int enqueue_sweep32_post(Ctx &c, int cur) {
+  TRY_RC(enqueue_cycle_update(c, 1, cur));
+  const size_t ncG = (size_t)c.nc * c.G;
+  const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
+  k_tally32<false><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi, nullptr);
+  UMT_CUDA(cudaGetLastError());
+  return 0;
+}
+
 // Whether an FP32 sweep of this context runs the zone-program kernel (the
 // kernel with the host-facing variant); prepares the FP32 records first.
 int fp32_program_path(Ctx &c, bool *yes) {

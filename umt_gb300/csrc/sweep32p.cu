@@ -83,8 +83,10 @@ __host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 
 
 // WT: also write the exiting rows, in FP64, to *p.psibOut (the variant used
 // by calls that return PsiB to the host; resident sweeps run the other).
+// One work item per team: the body of the stage kernels below.  blk is the
+// block's index among the blocks of this problem's stage.
 template <int GT, int GPL, bool WT>
-__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32p(ProgP p, int off, int nItems) {
+__device__ __forceinline__ void sweep_items(const ProgP &p, int off, int nItems, int blk) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
   constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
   constexpr int G = GT * GPL;
@@ -93,7 +95,7 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32p(ProgP p
   // The next stage's launch may start now: its blocks fill SMs as this
   // stage's finish and run their independent first two round trips.
   pdl_launch_dependents();
-  const int k = blockIdx.x * TEAMS + team;
+  const int k = blk * TEAMS + team;
   if (k >= nItems) return;                         // whole teams leave together
   const unsigned tm = team_mask(GT, tid);
   const int g0 = lane * GPL;
@@ -325,6 +327,33 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32p(ProgP p
       }
     }
   }
+}
+
+template <int GT, int GPL, bool WT>
+__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32p(ProgP p, int off, int nItems) {
+  sweep_items<GT, GPL, WT>(p, off, nItems, blockIdx.x);
+}
+
+// One dependency stage of several problems of the same group tile in one
+// launch: the blocks of problem j are [blockStart[j], blockStart[j+1]); each
+// problem brings its own parameters, stage offset and size.
+constexpr int PB_MAX = 64;
+struct ProgBatchP {
+  int n;
+  int blockStart[PB_MAX + 1];
+  int off[PB_MAX], cnt[PB_MAX];
+  ProgP p[PB_MAX];
+};
+
+template <int GT, int GPL>
+__global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32pm(const __grid_constant__ ProgBatchP b) {
+  int lo = 0, hi = b.n - 1;
+  const int bx = (int)blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (b.blockStart[mid] <= bx) lo = mid; else hi = mid - 1;
+  }
+  sweep_items<GT, GPL, false>(b.p[lo], b.off[lo], b.cnt[lo], bx - b.blockStart[lo]);
 }
 
 // ---------------------------------------------------------------------------
@@ -692,7 +721,8 @@ int prepare_prog32(Ctx &c) {
   c.progMaxChunks = (int)hf[1];
 #define UMT_ATTRP(gt, gpl)                                                    \
   TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, false>));      \
-  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, true>));
+  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, true>));       \
+  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32pm<gt, gpl>));
 #define TRY_RC_P(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
   UMT_ATTRP(1, 2) UMT_ATTRP(2, 2) UMT_ATTRP(4, 2) UMT_ATTRP(8, 2) UMT_ATTRP(16, 2) UMT_ATTRP(32, 2)
   UMT_ATTRP(1, 4) UMT_ATTRP(2, 4) UMT_ATTRP(4, 4) UMT_ATTRP(8, 4) UMT_ATTRP(16, 4) UMT_ATTRP(32, 4)
@@ -704,8 +734,8 @@ int prepare_prog32(Ctx &c) {
 
 // One launch per dependency stage.  Returns 1 when the tile or the context
 // has no program kernel (the caller then uses the corner-slot kernel).
-int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
-  if (c.progState != 1 || !sweep32p_supported(c.G, GT, GPL)) return 1;
+// The zone-program kernel's parameters for a context and buffer parity.
+static ProgP make_progp(const Ctx &c, int cur) {
   ProgP p;
   p.nz = c.nz; p.nc = c.nc; p.nb = c.nb;
   {
@@ -724,6 +754,12 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.homog32 ? c.psiB32h : c.psiB32;
   p.psibOut = c.psibOut;
   p.status = c.status;
+  return p;
+}
+
+int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
+  if (c.progState != 1 || !sweep32p_supported(c.G, GT, GPL)) return 1;
+  const ProgP p = make_progp(c, cur);
   const int TEAMS = P32_NT / GT;
   const size_t smem = (size_t)TEAMS * ((size_t)p.tstride * 4 + p.bstride);
   // Stage 0 follows the source conversion with ordinary stream order; every
@@ -763,6 +799,77 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   UMT_LAUNCHP(1, 4) UMT_LAUNCHP(2, 4) UMT_LAUNCHP(4, 4) UMT_LAUNCHP(8, 4) UMT_LAUNCHP(16, 4) UMT_LAUNCHP(32, 4)
 #undef UMT_LAUNCHP
   return 1;
+}
+
+// The stages of several resident FP32 sweeps that share one group tile
+// (GT, GPL), on stream st: stage s of every problem that has one goes into
+// one launch of k_sweep32pm (split every PB_MAX problems), each launch after
+// the first a programmatic dependent of the one before, as in a single
+// sweep.  Every context must be on the zone-program path (progState 1).
+int enqueue_batch_stages(const std::vector<Ctx *> &cs, const std::vector<int> &curs, int GT, int GPL,
+                         cudaStream_t st) {
+  if (cs.empty()) return 0;
+  const int G = GT * GPL, TEAMS = P32_NT / GT;
+  int maxStages = 0, bstride = 0;
+  for (const Ctx *c : cs) {
+    if (c->progState != 1 || c->G != G || !sweep32p_supported(c->G, GT, GPL))
+      return set_error(UMT_ERR_STATE, "batch stages: a context is not on the zone-program path of this tile");
+    maxStages = std::max(maxStages, c->sch.nStages);
+    bstride = std::max(bstride, blob_stride_p(c->progMaxChunks));
+  }
+  std::vector<ProgP> ps(cs.size());
+  for (size_t j = 0; j < cs.size(); ++j) {
+    ps[j] = make_progp(*cs[j], curs[j]);
+    ps[j].bstride = bstride;                       // one shared-memory layout for the launch
+  }
+  const size_t smem = (size_t)TEAMS * ((size_t)team_stride_p(G) * 4 + bstride);
+  cudaLaunchAttribute pdl[1];
+  pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  pdl[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(P32_NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  void (*kern)(ProgBatchP) = nullptr;
+#define UMT_PICKM(gt, gpl) if (GT == gt && GPL == gpl) kern = k_sweep32pm<gt, gpl>;
+  UMT_PICKM(1, 2) UMT_PICKM(2, 2) UMT_PICKM(4, 2) UMT_PICKM(8, 2) UMT_PICKM(16, 2) UMT_PICKM(32, 2)
+  UMT_PICKM(1, 4) UMT_PICKM(2, 4) UMT_PICKM(4, 4) UMT_PICKM(8, 4) UMT_PICKM(16, 4) UMT_PICKM(32, 4)
+#undef UMT_PICKM
+  if (!kern) return set_error(UMT_ERR_ARG, "batch stages: no kernel for tile %d x %d", GT, GPL);
+  std::vector<ProgBatchP> b(1);
+  bool first = true;
+  auto flush = [&](ProgBatchP &pb) -> int {
+    if (pb.n == 0) return 0;
+    cfg.gridDim = dim3(pb.blockStart[pb.n]);
+    cfg.attrs = first ? nullptr : pdl;
+    cfg.numAttrs = first ? 0 : 1;
+    first = false;
+    UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, pb));
+    pb.n = 0;
+    pb.blockStart[0] = 0;
+    return 0;
+  };
+  ProgBatchP &pb = b[0];
+  pb.n = 0;
+  pb.blockStart[0] = 0;
+  for (int s = 0; s < maxStages; ++s) {
+    for (size_t j = 0; j < cs.size(); ++j) {
+      const Ctx &c = *cs[j];
+      if (s >= c.sch.nStages || c.sch.hCount[s] <= 0) continue;
+      if (pb.n == PB_MAX) {
+        const int rf = flush(pb);
+        if (rf) return rf;
+      }
+      const int k = pb.n++;
+      pb.p[k] = ps[j];
+      pb.off[k] = c.sch.hOffset[s];
+      pb.cnt[k] = c.sch.hCount[s];
+      pb.blockStart[k + 1] = pb.blockStart[k] + (c.sch.hCount[s] + TEAMS - 1) / TEAMS;
+    }
+    const int rf = flush(pb);
+    if (rf) return rf;
+  }
+  return 0;
 }
 
 }  // namespace umt

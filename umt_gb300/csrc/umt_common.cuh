@@ -238,5 +238,9 @@ void free_psib(Ctx &c);
 int prepare_prog32(Ctx &c);
 bool sweep32p_supported(int G, int GT, int GPL);
 int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL);
+int enqueue_batch_stages(const std::vector<Ctx *> &cs, const std::vector<int> &curs, int GT, int GPL,
+                         cudaStream_t st);
+int enqueue_sweep32_pre(Ctx &c, int cur);
+int enqueue_sweep32_post(Ctx &c, int cur);
 
 }  // namespace umt
