@@ -355,8 +355,8 @@ def ttc_learned(args, lib):
     the FP64 GMRES answer (checked on the device after each iteration)."""
     from umt_gb300 import capi, learned
     t0 = time.perf_counter()
-    train = [learned.strongly_scattering_problem(3 + (k % 2), seed=5000 + k) for k in range(8)]
-    summary = learned.train_on_problems(lib, train, steps=1500, batch=4096, lr=2e-3)
+    train = [learned.strongly_scattering_problem(3 + (k % 2), seed=5000 + k) for k in range(args.train_problems)]
+    summary = learned.train_on_problems(lib, train, steps=args.train_steps, batch=4096, lr=2e-3)
     summary["wall_s"] = time.perf_counter() - t0
     prob = learned.strongly_scattering_problem(args.ttc_tiles, seed=5)
     learned.load_problem(lib, prob, flags=3 | 8)
@@ -373,12 +373,55 @@ def ttc_learned(args, lib):
                                          "converged", "learned_kept", "learned_rejected")}
     base = runs["fp64_plain"]["seconds"]
     best = runs["mixed_learned"]
-    return {"workload": f"strongly scattering, {args.ttc_tiles}^3 tiles ({prob.mesh.nzones} zones), 128 directions, "
+    heldout = heldout_eval(args, lib) if args.eval_seeds > 0 else None
+    return {"heldout": heldout,"workload": f"strongly scattering, {args.ttc_tiles}^3 tiles ({prob.mesh.nzones} zones), 128 directions, "
                         f"32 groups, seed 5", "target": "1e-6 relative L2 of PhiTotal vs FP64 GMRES (1e-10)",
             "reference_fp64_sweeps": n_ref, "reference_s": ref_s, "training": summary, "runs": runs,
             "speedup_mixed_learned_vs_fp64_plain": base / best["seconds"] if best["converged"] else None,
             "speedup_fp64_learned_vs_fp64_plain": base / runs["fp64_learned"]["seconds"],
             "time": "device seconds of umt103_source_iterate (CUDA events); wall_s is the host time of the call"}
+
+
+def heldout_eval(args, lib):
+    """The trained network on --eval-seeds held-out seeds (none used in
+    training) of the same distribution on --eval-tiles tiles per axis: each
+    problem is solved by FP64 GMRES (1e-10), then iterated from zero to 1e-6
+    relative L2 of that answer in FP64 and in the mixed form, each without and
+    with the learned step.  Reports the distribution over the seeds."""
+    from umt_gb300 import capi, learned
+    meth = (("fp64_plain", capi.UMT_FP64, 0), ("fp64_learned", capi.UMT_FP64, 5),
+            ("mixed_plain", capi.UMT_MIXED, 0), ("mixed_learned", capi.UMT_MIXED, 5))
+    rec = {m[0]: [] for m in meth}
+    t0 = time.perf_counter()
+    for k in range(args.eval_seeds):
+        prob = learned.strongly_scattering_problem(args.eval_tiles, seed=900000 + k)
+        learned.load_problem(lib, prob, flags=3 | 8)
+        phi_star, _ = learned.converged_phi(lib, prob)
+        for name, prec, le in meth:
+            r = learned.iterate_to(lib, prob, phi_star, precision=prec, learn_every=le, learn_start=3,
+                                   max_iters=4000 if prec != capi.UMT_MIXED else 60)
+            rec[name].append((r["iterations"], r["sweeps"], r["fp64_sweeps"], r["seconds"], bool(r["converged"]),
+                              r["learned_kept"], r["learned_rejected"]))
+
+    def stats(v):
+        v = sorted(v)
+        q = lambda f: v[min(len(v) - 1, int(f * (len(v) - 1) + 0.5))]
+        return {"min": v[0], "median": q(0.5), "p90": q(0.9), "max": v[-1], "mean": sum(v) / len(v)}
+
+    out = {"seeds": args.eval_seeds, "tiles": args.eval_tiles, "seed_range": [900000, 900000 + args.eval_seeds - 1],
+           "wall_s": time.perf_counter() - t0}
+    for name in rec:
+        rs = rec[name]
+        out[name] = {"converged": sum(r[4] for r in rs), "sweeps": stats([r[1] for r in rs]),
+                     "fp64_sweeps": stats([r[2] for r in rs]), "seconds": stats([r[3] for r in rs]),
+                     "learned_kept": sum(r[5] for r in rs), "learned_rejected": sum(r[6] for r in rs)}
+    ratio = lambda a, b, i: [x[i] / y[i] for x, y in zip(rec[a], rec[b])]
+    out["fp64_sweep_ratio_plain_over_learned"] = stats(ratio("fp64_plain", "fp64_learned", 1))
+    out["mixed_sweep_ratio_plain_over_learned"] = stats(ratio("mixed_plain", "mixed_learned", 1))
+    out["time_ratio_fp64_plain_over_mixed_learned"] = stats(ratio("fp64_plain", "mixed_learned", 3))
+    out["learned_helps_fp64"] = sum(1 for r in ratio("fp64_plain", "fp64_learned", 1) if r > 1.0)
+    out["learned_helps_mixed"] = sum(1 for r in ratio("mixed_plain", "mixed_learned", 1) if r > 1.0)
+    return out
 
 
 def run_rz(args):
@@ -624,6 +667,11 @@ def main():
     ap.add_argument("--shard", action="store_true",
                     help="time the angle-sharded source-iteration step (directions split over the ranks)")
     ap.add_argument("--ttc-tiles", type=int, default=6, help="--config 5: tiles per axis of the time-to-converge mesh")
+    ap.add_argument("--train-problems", type=int, default=8, help="--config 5: training problems (3 and 4 tiles per axis)")
+    ap.add_argument("--train-steps", type=int, default=1500, help="--config 5: Adam steps")
+    ap.add_argument("--eval-seeds", type=int, default=0,
+                    help="--config 5: also evaluate the trained network on this many held-out seeds")
+    ap.add_argument("--eval-tiles", type=int, default=3, help="--config 5: tiles per axis of the held-out problems")
     ap.add_argument("--gta", action="store_true", help="grey acceleration in the FP32 time-to-converge run")
     ap.add_argument("--gta-solver", type=int, default=1, choices=(1, 2),
                     help="with --gta: 1 grey + stretched-TSA sweeps, 2 grey sweep + per-zone direct solve")
