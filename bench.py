@@ -364,13 +364,16 @@ def ttc_learned(args, lib):
     phi_star, n_ref = learned.converged_phi(lib, prob)
     ref_s = time.perf_counter() - t1
     runs = {}
-    for name, prec, le in (("fp64_plain", capi.UMT_FP64, 0), ("fp64_learned", capi.UMT_FP64, 5),
-                           ("fp32_plain", capi.UMT_FP32, 0), ("mixed_plain", capi.UMT_MIXED, 0),
-                           ("mixed_learned", capi.UMT_MIXED, 5)):
+    lib.set_gta_solver(capi.UMT_GTA_ZONE)
+    lib.set_gta(10, 1e-4, 0)
+    for name, prec, le, gta in (("fp64_plain", capi.UMT_FP64, 0, False), ("fp64_learned", capi.UMT_FP64, 5, False),
+                                ("fp64_gta", capi.UMT_FP64, 0, True),
+                                ("fp32_plain", capi.UMT_FP32, 0, False), ("mixed_plain", capi.UMT_MIXED, 0, False),
+                                ("mixed_learned", capi.UMT_MIXED, 5, False)):
         r = learned.iterate_to(lib, prob, phi_star, precision=prec, learn_every=le, learn_start=3,
-                               max_iters=4000 if prec != capi.UMT_MIXED else 60)
+                               max_iters=4000 if prec != capi.UMT_MIXED else 60, use_gta=gta)
         runs[name] = {k: r[k] for k in ("iterations", "sweeps", "fp64_sweeps", "seconds", "wall_s", "error",
-                                         "converged", "learned_kept", "learned_rejected")}
+                                         "converged", "learned_kept", "learned_rejected", "grey_sweeps")}
     base = runs["fp64_plain"]["seconds"]
     best = runs["mixed_learned"]
     heldout = heldout_eval(args, lib) if args.eval_seeds > 0 else None
@@ -379,6 +382,8 @@ def ttc_learned(args, lib):
             "reference_fp64_sweeps": n_ref, "reference_s": ref_s, "training": summary, "runs": runs,
             "speedup_mixed_learned_vs_fp64_plain": base / best["seconds"] if best["converged"] else None,
             "speedup_fp64_learned_vs_fp64_plain": base / runs["fp64_learned"]["seconds"],
+            "speedup_fp64_gta_vs_fp64_plain": base / runs["fp64_gta"]["seconds"],
+            "gta": "newer solver (per-zone transfer matrices), 10 BiCGStab iterations at most, tolerance 1e-4",
             "time": "device seconds of umt103_source_iterate (CUDA events); wall_s is the host time of the call"}
 
 
