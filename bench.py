@@ -359,7 +359,7 @@ def ttc_learned(args, lib):
     summary = learned.train_on_problems(lib, train, steps=args.train_steps, batch=4096, lr=2e-3)
     summary["wall_s"] = time.perf_counter() - t0
     prob = learned.strongly_scattering_problem(args.ttc_tiles, seed=5)
-    learned.load_problem(lib, prob, flags=3 | 8)
+    learned.load_problem(lib, prob, flags=3)          # with the grey (GTA) context
     t1 = time.perf_counter()
     phi_star, n_ref = learned.converged_phi(lib, prob)
     ref_s = time.perf_counter() - t1

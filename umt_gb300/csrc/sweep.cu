@@ -251,6 +251,157 @@ __global__ void __launch_bounds__(SWEEP_NT) k_sweep(SweepP<T> p, int stage) {
   }
 }
 
+// The grey problem's sweep (one group, FP64: the GTA grey and zone-solve
+// sweeps).  With one group a (direction, zone) pair has no group loop to
+// spread over lanes, and one lane per pair made every stage as long as one
+// zone's serial chain of corner work.  Here a team of 8 lanes owns a pair,
+// lane c the zone's corner c: each lane stages its corner's faces, forms its
+// source and inflow, and computes the EZ closure of the faces its corner owns
+// (aez > 0) into shared memory.  Each corner then gathers the closures of
+// its own faces (+) and of its neighbours' faces toward it (-) in face order;
+// only the corner solve, in the schedule's corner order, runs one corner at a
+// time.  Arithmetic per face and corner is SweepUCBxyz.F90's (IEEE
+// division); the sums over a corner's faces are taken in face order rather
+// than in the reference's corner order.
+constexpr int GREY_NT = 128, GREY_GT = UMT_MAXCORNER;
+
+__global__ void __launch_bounds__(GREY_NT) k_sweep_grey(SweepP<double> p, int stage) {
+  constexpr int TEAMS = GREY_NT / GREY_GT;
+  __shared__ double s_Q[TEAMS][UMT_MAXCORNER], s_src[TEAMS][UMT_MAXCORNER], s_psi[TEAMS][UMT_MAXCORNER];
+  __shared__ double s_sez[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
+  __shared__ int8_t s_cez[TEAMS][UMT_MAXCORNER][UMT_MAXCF];
+  const int tid = threadIdx.x, team = tid / GREY_GT, c = tid % GREY_GT;
+  const int k = blockIdx.x * TEAMS + team;
+  if (k >= p.stageCount[stage]) return;            // whole teams leave together
+  const unsigned tm = 0xffu << ((tid & 31) / GREY_GT * GREY_GT);
+  uint32_t it = p.items[p.stageOffset[stage] + k];
+  const bool bad = (it >> 31) != 0;
+  it &= 0x7fffffffu;
+  const int a = (int)(it / (uint32_t)p.nz);
+  const int z = (int)(it - (uint32_t)a * p.nz);
+  const int nCorner = p.numCorner[z], c0 = p.cOffSet[z];
+  const uint32_t ord = p.order[it];
+  const size_t abase = (size_t)a * p.nc;
+  const bool own = c < nCorner;
+  const int cc = c0 + c;
+  double af[UMT_MAXCF] = {0.0, 0.0, 0.0}, ae[UMT_MAXCF] = {0.0, 0.0, 0.0}, psifp[UMT_MAXCF] = {0.0, 0.0, 0.0};
+  int cfp[UMT_MAXCF] = {0, 0, 0}, cez[UMT_MAXCF] = {0, 0, 0};
+  uint32_t in = 0, ex = 0, ezm = 0, opp = 0;
+  int ncf = 0;
+  double vol = 0.0, sum = 0.0, src = 0.0, Q = 0.0;
+  const double sig = p.Sigt[z];
+  if (own) {
+    ncf = p.nCFaces[cc];
+    vol = p.Volume[cc];
+#pragma unroll
+    for (int f = 0; f < UMT_MAXCF; ++f) {
+      af[f] = p.afp[(abase + cc) * UMT_MAXCF + f];
+      cfp[f] = p.cFP[cc * UMT_MAXCF + f];
+      if (f < ncf && af[f] > 0.0) { sum += af[f]; if (cfp[f] >= p.nc) ex |= 1u << f; }
+      if (f < ncf && af[f] < 0.0) in |= 1u << f;
+    }
+#pragma unroll
+    for (int f = 0; f < UMT_MAXCF; ++f) {
+      ae[f] = p.aez[(abase + cc) * UMT_MAXCF + f];
+      cez[f] = p.cEZ[cc * UMT_MAXCF + f];
+      s_cez[team][c][f] = (int8_t)(f < ncf ? cez[f] : -1);
+      if (f < ncf && ae[f] > 0.0) {
+        sum += ae[f];
+        ezm |= 1u << f;
+        if (ncf == 3 && af[(f + 1) % 3] < 0.0) opp |= 1u << f;
+      }
+    }
+    const double st = p.STotal ? p.STotal[cc] : 0.0;
+    Q = st + p.tau * p.psi_old[abase + cc];
+    src = vol * Q;
+    s_Q[team][c] = Q;
+#pragma unroll
+    for (int f = 0; f < UMT_MAXCF; ++f)
+      if ((in >> f) & 1u) {
+        const double pu = (cfp[f] < p.nc) ? p.psi_new[abase + cfp[f]]
+                                          : p.psiB[(size_t)a * p.nb + (cfp[f] - p.nc)];
+        psifp[f] = pu;
+        src = src - af[f] * pu;
+      }
+  }
+  __syncwarp(tm);
+  if (own) {
+#pragma unroll
+    for (int f = 0; f < UMT_MAXCF; ++f) {
+      s_sez[team][c][f] = 0.0;                     // faces this corner does not own
+      if (!((ezm >> f) & 1u)) continue;
+      const double aez = ae[f];
+      const double Qz = s_Q[team][cez[f]];
+      double sez;
+      if ((opp >> f) & 1u) {
+        const double psi_opp = psifp[(f + 1) % 3];
+        const double aez2 = aez * aez;
+        const double sigv = sig * vol;
+        const double sigv2 = sigv * sigv;
+        const double gnum = aez2 * (1.82 * sigv2 + aez * (4.0 * sigv + 3.0 * aez));
+        const double gden = vol * (4.0 * sigv * sigv2 + aez * (6.0 * sigv2 + 2.0 * aez * (2.0 * sigv + aez)));
+        sez = (vol * gnum * (sig * psi_opp - Q) + 0.5 * aez * gden * (Q - Qz)) / (gnum + gden * sig);
+      } else {
+        sez = 0.5 * aez * (1.0 / sig) * (Q - Qz);
+      }
+      s_sez[team][c][f] = sez;
+    }
+  }
+  __syncwarp(tm);
+  if (own) {
+#pragma unroll
+    for (int f = 0; f < UMT_MAXCF; ++f) {
+      if (f >= ncf) continue;
+      if ((ezm >> f) & 1u) {
+        src = src + s_sez[team][c][f];
+      } else if (ae[f] < 0.0) {
+        const int o = cez[f];                      // the neighbour corner owns this face
+        for (int g = 0; g < UMT_MAXCF; ++g)
+          if (s_cez[team][o][g] == c) { src = src - s_sez[team][o][g]; break; }
+      }
+    }
+    s_src[team][c] = src;
+  }
+  __syncwarp(tm);
+  double *out = p.psi_new + abase;
+  const double den = sum + sig * vol;
+  if (!bad) {
+    for (int i = 0; i < nCorner; ++i) {
+      if (c == (int)((ord >> (4 * i)) & 15u)) {
+        const double v = s_src[team][c] / den;
+        out[cc] = v;
+        s_psi[team][c] = v;
+#pragma unroll
+        for (int f = 0; f < UMT_MAXCF; ++f)
+          if ((ezm >> f) & 1u) s_src[team][cez[f]] += ae[f] * v;
+      }
+      __syncwarp(tm);
+    }
+  } else {
+    // direct solve with the previous iterate of this zone (SweepUCBxyz.F90:283-297)
+    for (int i = 0; i < nCorner; ++i) {
+      if (c == i) {
+        const double old = out[cc];
+#pragma unroll
+        for (int f = 0; f < UMT_MAXCF; ++f)
+          if ((ezm >> f) & 1u) s_src[team][cez[f]] += ae[f] * old;
+      }
+      __syncwarp(tm);
+    }
+    if (own) {
+      const double v = s_src[team][c] / den;
+      out[cc] = v;
+      s_psi[team][c] = v;
+    }
+  }
+  __syncwarp(tm);
+  if (own) {
+#pragma unroll
+    for (int f = 0; f < UMT_MAXCF; ++f)
+      if ((ex >> f) & 1u) p.psiB[(size_t)a * p.nb + (cfp[f] - p.nc)] = s_psi[team][c];
+  }
+}
+
 // psi -> phi tally: PhiTotal(g,c) = sum_a w_a psi_a(g,c), accumulated in FP64
 // (control/getPhiTotal_OMPOL.F90:63-131 does the same per direction).
 // FP32 angular flux: each thread owns 4 consecutive (corner, group) entries
@@ -412,6 +563,15 @@ static int enqueue_sweep(Ctx &c, int cur) {
     }
   }
   if constexpr (sizeof(T) == 8) TRY_RC(enqueue_cycle_init(c, prec, cur));
+  if constexpr (sizeof(T) == 8) {
+    if (c.G == 1 && !done) {                      // the grey problem: a team of lanes per pair, one per corner
+      for (int s = 0; s < c.sch.nStages; ++s) {
+        const int blocks = (c.sch.hCount[s] + GREY_NT / GREY_GT - 1) / (GREY_NT / GREY_GT);
+        k_sweep_grey<<<blocks, GREY_NT, 0, c.stream>>>(p, s);
+      }
+      done = true;
+    }
+  }
   for (int s = 0; s < c.sch.nStages && !done; ++s) {
     const int blocks = (c.sch.hCount[s] + TEAMS - 1) / TEAMS;
     switch (GT) {
