@@ -1265,7 +1265,7 @@ static int mixed_iterate(Ctx &c, const UmtSIParams *prm, const double *q, const 
     TRY(fetch2(c.red));
     st.rel = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
     double crit = st.rel;
-    if (ref) {                                    // T(X) is the better iterate: judge it
+    if (ref) {                                    // T(X) is the better iterate: measure it
       TRY(launch_distance(c, ref, c.red + 8));
       TRY(fetch2(c.red + 8));
       crit = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
