@@ -317,6 +317,68 @@ def test_fp32_sweep_pinned_psib_matches_pageable(umtlib):
     assert not np.array_equal(out[1][1], PsiB0)                   # exits were written back
 
 
+def test_fp32_sweep_source_chunks_follow_each_call(umtlib):
+    """The host-facing sweep converts a page-locked STotal in stage-ordered
+    chunks read straight from the caller's array, inside a graph that is
+    captured once and replayed.  A sequence of calls whose sources differ in
+    value and in how they arrive gives, call by call, the same PhiTotal, PsiB
+    and device source as the same sequence from pageable arrays.  The
+    sequence uses a new page-locked array, the same array refilled, no source
+    (zero), a page-locked array that is not 16-byte aligned (copied whole),
+    and a page-locked array again."""
+    torch = pytest.importorskip("torch")
+    prob = synthetic_problem((3, 3, 2), 2, 2, 8, seed=12, time_dependent=True)
+    m = prob.mesh
+    A, G = len(prob.weight), prob.ngr
+    rng = np.random.default_rng(21)
+    PsiB0 = rng.uniform(0.0, 0.1, size=(A, m.nbelem, G))
+    sources = [rng.uniform(0.05, 1.0, size=(m.ncornr, G)) for _ in range(4)]
+    kinds = ["new", "refill", "none", "unaligned", "new"]
+    values = [sources[0], sources[1], None, sources[2], sources[3]]
+
+    def pinned(shape, offset=0):
+        n = int(np.prod(shape))
+        buf = torch.empty(n + offset, dtype=torch.float64, pin_memory=True).numpy()
+        return buf[offset:offset + n].reshape(shape)
+
+    runs = []
+    for use_pinned in (False, True):
+        umtlib.init(m, prob.omega, prob.weight, G, flags=2 | 8)
+        umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+        umtlib.set_psi(prob.psi0, None)
+        PsiB = pinned((A, m.nbelem, G)) if use_pinned else np.empty((A, m.nbelem, G))
+        Phi = pinned((m.ncornr, G)) if use_pinned else np.empty((m.ncornr, G))
+        PsiB[...] = PsiB0
+        src = None
+        out = []
+        for kind, val in zip(kinds, values):
+            if val is None:
+                S = None
+            elif not use_pinned:
+                S = val.copy()
+            elif kind == "refill" and src is not None:
+                src[...] = val
+                S = src
+            elif kind == "unaligned":
+                S = pinned((m.ncornr, G), offset=1)
+                assert S.ctypes.data % 16 != 0
+                S[...] = val
+            else:
+                src = pinned((m.ncornr, G))
+                src[...] = val
+                S = src
+            umtlib.sweep(S, savePsi=True, PsiB=PsiB, precision=capi.UMT_FP32, Phi=Phi)
+            # the source the call left on the device drives a resident sweep
+            umtlib.sweep_resident(False, capi.UMT_FP32)
+            out.append((Phi.copy(), PsiB.copy(), umtlib.get_phi(m.ncornr, G)))
+        runs.append(out)
+    for k, (a, b) in enumerate(zip(*runs)):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), kinds[k]
+    # the calls differed: a zero source is not the first source
+    assert not np.array_equal(runs[1][0][0], runs[1][2][0])
+
+
 def test_autotuner_picks_the_fastest_tile_and_keeps_results(umtlib):
     """umt103_autotune times every group tile, keeps the fastest, and the
     tuned sweep equals a sweep with that tile set by hand (bit for bit) and

@@ -836,8 +836,6 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   if (precision == UMT_FP64 && !c.psi64[0]) return set_error(UMT_ERR_STATE, "FP64 flux not allocated");
   if (precision == UMT_FP32 && !c.psi32[0]) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   const size_t ncG = (size_t)c.nc * c.G, psiBN = (size_t)c.A * c.nb * c.G;
-  if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
-  else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
   // FP32: only the PsiB rows a sweep reads go in and only the rows it writes
   // come out, so the caller's array keeps its other rows bit for bit.
   // Page-locked host memory is read and written by the kernels directly;
@@ -846,13 +844,14 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
   // read from host memory by the stage kernels (that put the link's latency
   // on every boundary item's dependency chain and was slower).  With the
   // zone-program kernel that copy runs in stage-ordered chunks beside the
-  // stages, the sweep writes the exiting rows to the FP64 array as it goes
-  // (its host-facing variant), and the tally writes PhiTotal straight to a
-  // page-locked destination.
-  double *psibHost = nullptr, *psibFP64 = nullptr, *phiHost = nullptr;
-  bool psibWT = false, wt = false;
+  // stages, the exiting rows go to the FP64 array in chunks after the stages
+  // that write them, and the tally writes PhiTotal straight to a page-locked
+  // destination.  A page-locked STotal is converted in stage-ordered chunks
+  // beside the stages too, instead of being copied whole before the first
+  // stage.
+  double *psibHost = nullptr, *psibFP64 = nullptr, *phiHost = nullptr, *srcHost = nullptr;
+  bool psibWT = false, wt = false, prog = false;
   if (precision == UMT_FP32 && (PsiB_inout || PhiTotal_out)) {
-    bool prog = false;
     TRY(fp32_program_path(c, &prog));
     if (PsiB_inout) {
       TRY(ensure_bface(c));
@@ -872,25 +871,39 @@ int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out, double
     // the host-facing graph copies the rows the sweep reads in stage-ordered
     // chunks beside the stages (psib.cu); otherwise they go in first
     if (wt) TRY(ensure_psib_order(c));
+    if (wt && prog) {
+      TRY(ensure_src_order(c));
+      srcHost = STotal ? mapped_host(const_cast<double *>(STotal)) : nullptr;   // read only
+      if ((uintptr_t)srcHost & 15u) srcHost = nullptr;
+    }
     if (PsiB_inout && !psibWT)
       k_psib_rows<<<4096, 256, 0, c.stream>>>(c.A, c.nb, c.nc, c.G, c.bFace, c.afp32, psibFP64, c.psiB32, nullptr, 0);
     if (wt) {
       k_set_word<<<1, 1, 0, c.stream>>>(c.psibIn, psibWT ? psibFP64 : nullptr);
       k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, psibWT ? psibFP64 : nullptr);
       k_set_word<<<1, 1, 0, c.stream>>>(c.phiOut, phiHost);
+      if (c.srcIn) k_set_word<<<1, 1, 0, c.stream>>>(c.srcIn, srcHost);
     }
     UMT_CUDA(cudaGetLastError());
   } else if (PsiB_inout) {
     UMT_CUDA(cudaMemcpyAsync(c.psiB64, PsiB_inout, psiBN * 8, cudaMemcpyHostToDevice, c.stream));
   }
+  // the device's FP64 source: copied here, or filled from srcHost by the chunks
+  if (!srcHost) {
+    if (STotal) UMT_CUDA(cudaMemcpyAsync(c.STotal, STotal, ncG * 8, cudaMemcpyHostToDevice, c.stream));
+    else UMT_CUDA(cudaMemsetAsync(c.STotal, 0, ncG * 8, c.stream));
+  }
   c.wantExitsThrough = wt;
+  c.wantSrcChunks = wt && prog;
   const int rcs = sweep_core(savePsi, precision);
   const bool wrote = psibWT && c.exitsThrough;
   c.wantExitsThrough = false;
+  c.wantSrcChunks = false;
   if (wt) {                                        // resident sweeps touch no host memory
     k_set_word<<<1, 1, 0, c.stream>>>(c.psibIn, nullptr);
     k_set_word<<<1, 1, 0, c.stream>>>(c.psibOut, nullptr);
     k_set_word<<<1, 1, 0, c.stream>>>(c.phiOut, nullptr);
+    if (c.srcIn) k_set_word<<<1, 1, 0, c.stream>>>(c.srcIn, nullptr);
   }
   TRY(rcs);
   if (PhiTotal_out && !phiHost) UMT_CUDA(cudaMemcpyAsync(PhiTotal_out, c.Phi, ncG * 8, cudaMemcpyDeviceToHost, c.stream));

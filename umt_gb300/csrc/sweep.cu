@@ -547,9 +547,18 @@ static int enqueue_sweep(Ctx &c, int cur) {
     c.exitsThrough = false;                   // set again by the zone-program path below
     const size_t n = (size_t)c.nz * c.G;
     k_to_float<<<(int)std::min<size_t>((n + 255) / 256, 4096), 256, 0, c.stream>>>(n, c.Sigt, c.Sigt32);
-    const size_t m = (size_t)c.nc * c.G;
-    k_to_float<<<(int)std::min<size_t>((m + 255) / 256, 4096), 256, 0, c.stream>>>(m, c.STotal, c.STotal32);
     if (c.tileGT == 0) default_tile(c.G, &c.tileGT, &c.tileGPL);
+    // the host-facing zone-program sweep converts the source in stage-ordered
+    // chunks beside its stages (enqueue_psib_chunks); every other sweep here
+    const bool srcChunks = c.wantExitsThrough && c.wantSrcChunks && c.srcOrder && c.rec32Ready &&
+                           c.sweepMode == 0 && c.progState == 1 && c.tileGT > 0 &&
+                           sweep32_supported(c.G, c.tileGT, c.tileGPL) &&
+                           sweep32p_supported(c.G, c.tileGT, c.tileGPL);
+    if (!srcChunks) {
+      const size_t m = (size_t)c.nc * c.G;
+      k_to_float<<<(int)std::min<size_t>((m + 255) / 256, 4096), 256, 0, c.stream>>>(m, c.STotal, c.STotal32);
+    }
+    c.srcChunksNow = srcChunks;
     TRY_RC(enqueue_cycle_init(c, prec, cur));
     if (c.tileGT > 0 && sweep32_supported(c.G, c.tileGT, c.tileGPL)) {
       if (!c.rec32Ready) {
@@ -588,9 +597,11 @@ static int enqueue_sweep(Ctx &c, int cur) {
   const size_t ncG = (size_t)c.nc * c.G;
   const int tb = (int)std::min<size_t>((ncG / 4 + 255) / 256 + 1, 152 * 16);
   if constexpr (sizeof(T) == 4) {
-    if (c.wantExitsThrough)
+    if (c.wantExitsThrough) {
       k_tally32<true><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi, c.phiOut);
-    else
+      // the last exit chunks are copied out beside the tally
+      if (c.exitsThrough) TRY_RC(join_exit_chunks(c));
+    } else
       k_tally32<false><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight32, c.psi32[1 - cur], c.Phi, nullptr);
   } else {
     k_tally<double><<<tb, 256, 0, c.stream>>>(c.A, ncG, c.weight, c.psi64[1 - cur], c.Phi);
@@ -624,7 +635,7 @@ int enqueue_sweep32_post(Ctx &c, int cur) {
 }
 
 // Whether an FP32 sweep of this context runs the zone-program kernel (the
-// kernel with the host-facing variant); prepares the FP32 records first.
+// path of the chunked host-facing graph); prepares the FP32 records first.
 int fp32_program_path(Ctx &c, bool *yes) {
   TRY_RC(prepare_precision(c, 1));
   *yes = c.sweepMode == 0 && c.progState == 1 && c.tileGT > 0 && sweep32_supported(c.G, c.tileGT, c.tileGPL) &&

@@ -476,7 +476,7 @@ int enqueue_sweep32(Ctx &c, int cur, int GT, int GPL) {
   c.exitsThrough = false;
   if (c.sweepMode == 0) {
     const int rc = enqueue_sweep32p(c, cur, GT, GPL);
-    if (rc == 0) c.exitsThrough = true;            // the program kernel writes *psibOut's rows
+    if (rc == 0) c.exitsThrough = true;            // the exit chunks write *psibOut's rows
     if (rc <= 0) return rc;                        // 1: no program kernel for this tile
   }
 #define UMT_LAUNCH32(gt, gpl)                                                                      \

@@ -55,7 +55,6 @@ struct ProgP {
   float tau;
   const float *psi_old;
   float *psi_new, *psiB;
-  double *const *psibOut;               // device word: FP64 copy of the exiting PsiB rows, or null
   unsigned *status;                     // device status word (a copy that never completed)
 };
 
@@ -81,11 +80,12 @@ __device__ __forceinline__ float2 div2(float2 a, float2 b) {
 // pair padded to a whole number of 32-bank spans.
 __host__ __device__ constexpr int pair_stride(int G) { return (2 * G + 31) / 32 * 32; }
 
-// WT: also write the exiting rows, in FP64, to *p.psibOut (the variant used
-// by calls that return PsiB to the host; resident sweeps run the other).
 // One work item per team: the body of the stage kernels below.  blk is the
-// block's index among the blocks of this problem's stage.
-template <int GT, int GPL, bool WT>
+// block's index among the blocks of this problem's stage.  Calls that return
+// PsiB to the host run the same kernel; their exiting rows are copied out of
+// the device rows in chunks beside the stages (psib.cu), so no stage waits
+// for stores to host memory to complete.
+template <int GT, int GPL>
 __device__ __forceinline__ void sweep_items(const ProgP &p, int off, int nItems, int blk) {
   static_assert(GPL == 2 || GPL == 4, "group pairs");
   constexpr int TEAMS = P32_NT / GT, NP = GPL / 2, NFC = GPL == 2 ? 12 : 8;
@@ -304,34 +304,18 @@ __device__ __forceinline__ void sweep_items(const ProgP &p, int off, int nItems,
     st2<NP>(res + c * RP + g0, v);
     st2<NP>(psiNew + (size_t)(c0 + c) * G, v);
   }
-  // exiting boundary fluxes; with WT the same rows also go, in FP64, to the
-  // caller's PsiB (page-locked host memory) or its staging copy when one is set
-  double *hbA = nullptr;
-  if constexpr (WT) {
-    if (nX) {
-      double *const hb = *p.psibOut;             // read here: nothing stays live across the solve
-      hbA = hb ? hb + (size_t)a * p.nb * G + g0 : nullptr;
-    }
-  }
+  // exiting boundary fluxes
   for (int x = 0; x < nX; ++x) {
     const uint32_t e = ex[x];
     float2 v[NP];
     ld2<NP>(res + (int)((e >> 28) & 7u) * RP + g0, v);
-    const size_t b = (size_t)(e & 0x0fffffffu);
-    st2<NP>(psiBA + b * G, v);
-    if constexpr (WT) {
-      if (hbA) {
-#pragma unroll
-        for (int q = 0; q < NP; ++q)
-          *reinterpret_cast<double2 *>(hbA + b * G + 2 * q) = make_double2((double)v[q].x, (double)v[q].y);
-      }
-    }
+    st2<NP>(psiBA + (size_t)(e & 0x0fffffffu) * G, v);
   }
 }
 
-template <int GT, int GPL, bool WT>
+template <int GT, int GPL>
 __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32p(ProgP p, int off, int nItems) {
-  sweep_items<GT, GPL, WT>(p, off, nItems, blockIdx.x);
+  sweep_items<GT, GPL>(p, off, nItems, blockIdx.x);
 }
 
 // One dependency stage of several problems of the same group tile in one
@@ -353,7 +337,7 @@ __global__ void __launch_bounds__(P32_NT, GPL == 2 ? 14 : 12) k_sweep32pm(const 
     const int mid = (lo + hi + 1) >> 1;
     if (b.blockStart[mid] <= bx) lo = mid; else hi = mid - 1;
   }
-  sweep_items<GT, GPL, false>(b.p[lo], b.off[lo], b.cnt[lo], bx - b.blockStart[lo]);
+  sweep_items<GT, GPL>(b.p[lo], b.off[lo], b.cnt[lo], bx - b.blockStart[lo]);
 }
 
 // ---------------------------------------------------------------------------
@@ -720,8 +704,7 @@ int prepare_prog32(Ctx &c) {
   c.progBytes = (size_t)total * 16;
   c.progMaxChunks = (int)hf[1];
 #define UMT_ATTRP(gt, gpl)                                                    \
-  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, false>));      \
-  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl, true>));       \
+  TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32p<gt, gpl>));            \
   TRY_RC_P(allow_dynamic_smem((const void *)k_sweep32pm<gt, gpl>));
 #define TRY_RC_P(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
   UMT_ATTRP(1, 2) UMT_ATTRP(2, 2) UMT_ATTRP(4, 2) UMT_ATTRP(8, 2) UMT_ATTRP(16, 2) UMT_ATTRP(32, 2)
@@ -752,7 +735,6 @@ static ProgP make_progp(const Ctx &c, int cur) {
   p.hdr = (const uint4 *)c.hdr32; p.prog = (const uint4 *)c.prog32;
   p.Sigt = c.Sigt32; p.STotal = c.STotal32; p.tau = c.homog32 ? 0.f : (float)c.tau;
   p.psi_old = c.psi32[cur]; p.psi_new = c.psi32[1 - cur]; p.psiB = c.homog32 ? c.psiB32h : c.psiB32;
-  p.psibOut = c.psibOut;
   p.status = c.status;
   return p;
 }
@@ -773,8 +755,7 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
   cfg.stream = c.stream;
 #define UMT_LAUNCHP(gt, gpl)                                                                   \
   if (GT == gt && GPL == gpl) {                                                                \
-    void (*kern)(ProgP, int, int) = c.wantExitsThrough ? k_sweep32p<gt, gpl, true>                  \
-                                                  : k_sweep32p<gt, gpl, false>;                \
+    void (*kern)(ProgP, int, int) = k_sweep32p<gt, gpl>;                                       \
     if (c.wantExitsThrough) {                                                                  \
       const int rq = enqueue_psib_chunks(c);                                                   \
       if (rq) return rq;                                                                       \
@@ -787,7 +768,11 @@ int enqueue_sweep32p(Ctx &c, int cur, int GT, int GPL) {
       cfg.gridDim = dim3((c.sch.hCount[s] + TEAMS - 1) / TEAMS);                               \
       cfg.attrs = s > 0 && c.usePDL ? pdl : nullptr;                                           \
       cfg.numAttrs = s > 0 && c.usePDL ? 1 : 0;                                                \
-      UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p, c.sch.hOffset[s], c.sch.hCount[s]));                                          \
+      UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, p, c.sch.hOffset[s], c.sch.hCount[s]));          \
+      if (c.wantExitsThrough) {                                                                \
+        const int rq = enqueue_exit_chunks(c, s);                                              \
+        if (rq) return rq;                                                                     \
+      }                                                                                        \
     }                                                                                          \
     if (c.wantExitsThrough) {                                                                  \
       const int rq = wait_psib_chunks(c, c.sch.nStages);                                       \

@@ -126,20 +126,33 @@ struct Ctx {
   double *scratch = nullptr;                    // reductions
   size_t scratchBytes = 0;
   int *bFace = nullptr;                         // [nb] corner face c*3 + f of each boundary element (-1: none)
-  double **psibOut = nullptr;                   // device word read by the zone-program kernel's host-facing
-                                                // variant: FP64 destination of the exiting PsiB rows, or null
+  double **psibOut = nullptr;                   // device word read by the exit-row copies of the host-facing
+                                                // graph: FP64 destination of the exiting PsiB rows, or null
   double **phiOut = nullptr;                    // device word: FP64 PhiTotal destination of the tally, or null
   bool exitsThrough = false;                    // the FP32 sweep as enqueued runs the zone-program kernel
-  bool wantExitsThrough = false;                // enqueue the host-facing variants (zone program, tally)
+  bool wantExitsThrough = false;                // enqueue the host-facing graph (row chunks, host-writing tally)
   cudaGraphExec_t graphsWT[2] = {nullptr, nullptr};   // FP32 sweeps of those variants, [cur]
   // PsiB rows the sweep does not write, ordered by the stage that reads them
   // (psib.cu), copied in chunks on a side stream inside the host-facing graph
   int *rowOrder = nullptr;                      // row indices a*nb + b
   std::vector<int> chunkOff, chunkStage;        // chunk k: rowOrder[chunkOff[k], chunkOff[k+1]), read from stage chunkStage[k]
   double **psibIn = nullptr;                    // device word: the FP64 rows to copy (host or staging), or null
-  cudaStream_t stream2 = nullptr;
-  cudaEvent_t evFork = nullptr;
-  std::vector<cudaEvent_t> evChunk;
+  // The source rows (corners) in the same stage-ordered chunks, by the first
+  // stage over all directions that sweeps the corner's zone; the host-facing
+  // graph converts STotal chunk by chunk instead of all before stage 0
+  int *srcOrder = nullptr;                      // corner indices
+  std::vector<int> srcChunkOff, srcChunkStage;
+  double **srcIn = nullptr;                     // device word: page-locked FP64 STotal, or null (convert the device copy)
+  bool wantSrcChunks = false;                   // enqueue the chunked source conversion (host-facing zone-program graph)
+  bool srcChunksNow = false;                    // the sweep being enqueued converts the source that way
+  // The exiting PsiB rows ordered by the stage that writes them; the
+  // host-facing graph copies them to *psibOut in chunks on a third stream,
+  // each after the last stage that writes one of its rows
+  int *exitOrder = nullptr;                     // row indices a*nb + b
+  std::vector<int> exitChunkOff, exitChunkLast; // chunk k: exitOrder[off[k], off[k+1]), complete after stage last[k]
+  cudaStream_t stream2 = nullptr, stream3 = nullptr;
+  cudaEvent_t evFork = nullptr, evExitJoin = nullptr;
+  std::vector<cudaEvent_t> evChunk, evSrc, evExit;
   double *stage64 = nullptr;                    // FP64 staging of PsiB for FP32 sweeps (kept)
   size_t stage64N = 0;
   // captured sweep graphs per precision
@@ -231,8 +244,15 @@ int fp32_program_path(Ctx &c, bool *yes);
 // PsiB rows between host arrays and the device copy (psib.cu)
 int ensure_bface(Ctx &c);
 int ensure_psib_order(Ctx &c);
+int ensure_src_order(Ctx &c);
+// the host-facing graph's side-stream chunks (PsiB rows, and the source rows
+// when c.srcChunksNow), and the waits of stage s on those that begin there
 int enqueue_psib_chunks(Ctx &c);
 int wait_psib_chunks(Ctx &c, int stage);
+// after the launch of stage s: copy out the exit chunks complete there; after
+// the tally: join those copies
+int enqueue_exit_chunks(Ctx &c, int stage);
+int join_exit_chunks(Ctx &c);
 void free_psib(Ctx &c);
 // zone-program FP32 kernel (sweep32p.cu)
 int prepare_prog32(Ctx &c);
