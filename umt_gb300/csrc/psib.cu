@@ -21,8 +21,6 @@
 
 #include <algorithm>
 
-#define TRY_RC(x) do { int rc_ = (x); if (rc_) return rc_; } while (0)
-
 namespace umt {
 
 // Boundary element b's corner face c*3 + f (cFP holds nc + b on boundary faces).
@@ -106,8 +104,8 @@ __global__ void __launch_bounds__(256) k_rows_out(const int *rows, int n, int G,
 // *src (page-locked host memory or a device staging copy, 16-byte aligned)
 // into the FP32 copy dst32, G even.  With *src null: nothing (PsiB), or, with
 // SRC, the rows of the device copy dev64.  With SRC and a host array the rows
-// also go to dev64, which keeps the FP64 source of the call as the copy
-// before it did.  It runs beside the latency-bound stage kernels, so it uses
+// also go to dev64, so the device keeps the call's FP64 source as a copy of
+// the whole array would.  It runs beside the latency-bound stage kernels, so it uses
 // few blocks (PSIB_GATHER_BLOCKS) and keeps 8 pairs of values in flight per
 // thread instead: 64 blocks hold ~2 MB in flight (24 blocks, ~0.8 MB, reached
 // only ~110 GB/s of the link's ~210 under its loaded latency).
@@ -169,13 +167,13 @@ __global__ void k_corner_scatter(int nc, int nStages, const int *cToZone, const 
 }
 
 // Chunks of a list ordered by stage (start[s] = first entry of stage s),
-// cut at stage boundaries into pieces of about CHUNK_ROWS_TARGET rows (and
-// at least 1/CHUNK_MAX of the list), the empty ones left out; chunk k is
-// waited for by the first stage that reads one of its rows.  With tail, the
-// entries past the last stage (rows no stage reads) are one more chunk,
-// waited for at the end of the sweep.  Chunks that double in stage span made
-// stage 2^k wait for every row read up to stage 2^(k+1): at 20^3 tiles the
-// middle stages then waited milliseconds for the link.
+// cut at stage boundaries into pieces of at least about 4 MB of FP64 rows
+// and at least 1/CHUNK_MAX of the list, the empty ones left out.  stage[k]
+// is the first stage with a row in chunk k, (*last)[k] the last one.  With
+// tail, the entries past the last stage (rows no stage reads) are one more
+// chunk, waited for at the end of the sweep.  Small chunks matter: with
+// chunks of doubling stage span, stage 2^k would wait for every row read up
+// to stage 2^(k+1), milliseconds of link time at 20^3 tiles.
 constexpr int CHUNK_MAX = 96;
 static void stage_chunks(const std::vector<int> &start, int S, bool tail, int G, std::vector<int> &off,
                          std::vector<int> &stage, std::vector<int> *last = nullptr) {
@@ -257,48 +255,60 @@ static int ensure_exit_order(Ctx &c) {
                                      order);
   const cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return fail(set_error(UMT_ERR_CUDA, "exit row order: %s", cudaGetErrorString(e)));
-  cudaFree(count);
-  c.exitOrder = order;
   std::vector<int> firstStage;
   stage_chunks(start, S, false, c.G, c.exitChunkOff, firstStage, &c.exitChunkLast);
-  if (!c.stream3) UMT_CUDA(cudaStreamCreateWithFlags(&c.stream3, cudaStreamNonBlocking));
-  if (!c.evExitJoin) UMT_CUDA(cudaEventCreateWithFlags(&c.evExitJoin, cudaEventDisableTiming));
-  return ensure_events(c.evExit, c.exitChunkLast.size());
+  if (!c.stream3 && cudaStreamCreateWithFlags(&c.stream3, cudaStreamNonBlocking) != cudaSuccess) {
+    c.stream3 = nullptr;
+    return fail(set_error(UMT_ERR_CUDA, "exit row order: stream creation failed"));
+  }
+  if (!c.evExitJoin && cudaEventCreateWithFlags(&c.evExitJoin, cudaEventDisableTiming) != cudaSuccess) {
+    c.evExitJoin = nullptr;
+    return fail(set_error(UMT_ERR_CUDA, "exit row order: event creation failed"));
+  }
+  const int re = ensure_events(c.evExit, c.exitChunkLast.size());
+  if (re) return fail(re);
+  cudaFree(count);
+  c.exitOrder = order;                             // kept only once its chunks, stream and events exist
+  return 0;
 }
 
 int ensure_psib_order(Ctx &c) {
-  if (c.rowOrder) return 0;
+  if (c.rowOrder) return ensure_exit_order(c);
   if (!c.afp32 || !c.psiB32) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   if ((long long)c.A * c.nb >= (1LL << 31)) return set_error(UMT_ERR_ARG, "PsiB rows exceed 2^31");
   int rc = ensure_bface(c);
   if (rc) return rc;
   const int S = c.sch.nStages;
-  int *count = nullptr;
+  int *count = nullptr, *order = nullptr;
   if (cudaMalloc((void **)&count, (size_t)(S + 1) * sizeof(int)) != cudaSuccess)
     return set_error(UMT_ERR_NOMEM, "PsiB row order: allocation failed");
-  UMT_CUDA(cudaMemset(count, 0, (size_t)(S + 1) * sizeof(int)));
+  // the order is kept (c.rowOrder) only once it, its chunks and their events exist
+  auto fail = [&](int rc_) { cudaFree(count); if (order) cudaFree(order); return rc_; };
+  cudaMemset(count, 0, (size_t)(S + 1) * sizeof(int));
   k_row_count<false><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count);
   std::vector<int> h(S + 1);
-  UMT_CUDA(cudaMemcpy(h.data(), count, (size_t)(S + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+  if (cudaMemcpy(h.data(), count, (size_t)(S + 1) * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(set_error(UMT_ERR_CUDA, "PsiB row order: %s", cudaGetErrorString(cudaGetLastError())));
   std::vector<int> start(S + 2, 0);
   for (int s = 0; s <= S; ++s) start[s + 1] = start[s] + h[s];
   const int total = start[S + 1];
-  if (cudaMalloc((void **)&c.rowOrder, (size_t)std::max(total, 1) * sizeof(int)) != cudaSuccess) {
-    cudaFree(count);
-    c.rowOrder = nullptr;
-    return set_error(UMT_ERR_NOMEM, "PsiB row order: allocation failed");
+  if (cudaMalloc((void **)&order, (size_t)std::max(total, 1) * sizeof(int)) != cudaSuccess) {
+    order = nullptr;
+    return fail(set_error(UMT_ERR_NOMEM, "PsiB row order: allocation failed"));
   }
-  UMT_CUDA(cudaMemcpy(count, start.data(), (size_t)(S + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  cudaMemcpy(count, start.data(), (size_t)(S + 1) * sizeof(int), cudaMemcpyHostToDevice);
   k_row_scatter<false><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count,
-                                      c.rowOrder);
-  UMT_CUDA(cudaGetLastError());
-  UMT_CUDA(cudaDeviceSynchronize());
-  cudaFree(count);
+                                      order);
+  const cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return fail(set_error(UMT_ERR_CUDA, "PsiB row order: %s", cudaGetErrorString(e)));
   // chunks of ~4 MB or more in stage order, then the rows no stage reads
   stage_chunks(start, S, true, c.G, c.chunkOff, c.chunkStage);
-  TRY_RC(ensure_side_stream(c));
-  TRY_RC(ensure_events(c.evChunk, c.chunkStage.size()));
-  TRY_RC(alloc_word(&c.psibIn, "PsiB source word"));
+  int re = ensure_side_stream(c);
+  if (!re) re = ensure_events(c.evChunk, c.chunkStage.size());
+  if (!re) re = alloc_word(&c.psibIn, "PsiB source word");
+  if (re) return fail(re);
+  cudaFree(count);
+  c.rowOrder = order;
   return ensure_exit_order(c);
 }
 
@@ -315,7 +325,7 @@ int ensure_src_order(Ctx &c) {
     return set_error(UMT_ERR_NOMEM, "source row order: allocation failed");
   }
   int *order = nullptr;
-  // the order is kept (c.srcOrder) only once it is complete
+  // the order is kept (c.srcOrder) only once it, its chunks and their events exist
   auto fail = [&](int rc) { cudaFree(first); cudaFree(count); if (order) cudaFree(order); return rc; };
   if (cudaMalloc((void **)&order, (size_t)std::max(c.nc, 1) * sizeof(int)) != cudaSuccess) {
     order = nullptr;
@@ -336,13 +346,15 @@ int ensure_src_order(Ctx &c) {
                                                                                  order);
   const cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return fail(set_error(UMT_ERR_CUDA, "source row order: %s", cudaGetErrorString(e)));
+  stage_chunks(start, S, false, c.G, c.srcChunkOff, c.srcChunkStage);
+  int re = ensure_side_stream(c);
+  if (!re) re = ensure_events(c.evSrc, c.srcChunkStage.size());
+  if (!re) re = alloc_word(&c.srcIn, "source word");
+  if (re) return fail(re);
   cudaFree(first);
   cudaFree(count);
   c.srcOrder = order;
-  stage_chunks(start, S, false, c.G, c.srcChunkOff, c.srcChunkStage);
-  TRY_RC(ensure_side_stream(c));
-  TRY_RC(ensure_events(c.evSrc, c.srcChunkStage.size()));
-  return alloc_word(&c.srcIn, "source word");
+  return 0;
 }
 
 // Inside the host-facing graph: fork the chunk copies onto the side stream,
