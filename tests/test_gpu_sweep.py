@@ -1,4 +1,6 @@
 """GPU parity: the CUDA sweep through the C-ABI against the CPU oracle."""
+import os
+
 import numpy as np
 import pytest
 
@@ -377,6 +379,60 @@ def test_fp32_sweep_source_chunks_follow_each_call(umtlib):
             assert np.array_equal(x, y), kinds[k]
     # the calls differed: a zero source is not the first source
     assert not np.array_equal(runs[1][0][0], runs[1][2][0])
+
+
+def test_host_facing_chunks_at_128_directions_match_resident_sweep(umtlib):
+    """At 10^3 tiles, 128 directions and 16 groups, the host-facing call
+    splits its row lists into many chunks: about 47 of incoming PsiB rows, 5
+    of source rows and 47 of exiting rows, each waited for or copied at its
+    own stage.  Two calls with page-locked buffers and different sources (the
+    second a graph replay) give the PhiTotal and the exiting rows of the
+    resident sweep, which converts everything before stage 0, bit for bit.
+    Every other row of the caller's PsiB keeps its input."""
+    torch = pytest.importorskip("torch")
+    t, G = 10, 16
+    prob = synthetic_problem((t,) * 3, 4, 4, G, seed=31, time_dependent=True)
+    m = prob.mesh
+    A = len(prob.weight)
+    need = 3 * A * m.ncornr * G * 8                    # the device flux fetched as FP64, plus headroom
+    try:
+        avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+    except (ValueError, OSError, AttributeError):
+        avail = None
+    if avail is not None and avail < need:
+        pytest.skip(f"needs ~{need / 1e9:.0f} GB of free host memory")
+    rng = np.random.default_rng(32)
+    PsiB0 = rng.uniform(0.0, 0.1, size=(A, m.nbelem, G))
+    sources = [rng.uniform(0.05, 1.0, size=(m.ncornr, G)) for _ in range(2)]
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    # resident references: the whole source and PsiB converted before stage 0
+    umtlib.init(m, prob.omega, prob.weight, G, flags=2 | 8)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    refs = []
+    for S in sources:
+        umtlib.set_psi(prob.psi0, PsiB0)
+        umtlib.set_source(S)
+        umtlib.sweep_resident(False, capi.UMT_FP32)
+        _, PsiB_dev = umtlib.get_psi(capi.UMT_FP32)
+        refs.append((umtlib.get_phi(m.ncornr, G), PsiB_dev))
+    # host-facing calls on a fresh context
+    umtlib.init(m, prob.omega, prob.weight, G, flags=2 | 8)
+    umtlib.set_materials(prob.sigt, prob.sigs, prob.tau)
+    umtlib.set_psi(prob.psi0, None)
+    PsiB, Phi, Sh = pinned((A, m.nbelem, G)), pinned((m.ncornr, G)), pinned((m.ncornr, G))
+    for S, (phi_ref, psib_ref) in zip(sources, refs):
+        PsiB[...] = PsiB0
+        Sh[...] = S
+        umtlib.sweep(Sh, savePsi=False, PsiB=PsiB, precision=capi.UMT_FP32, Phi=Phi)
+        assert np.array_equal(Phi, phi_ref)
+        kept = np.all(PsiB == PsiB0, axis=2)
+        assert np.array_equal(PsiB[~kept], psib_ref[~kept])
+        ex, tot = umtlib.psib_rows()
+        assert (~kept).sum() == ex and tot == A * m.nbelem
+    umtlib.finalize()
 
 
 def test_autotuner_picks_the_fastest_tile_and_keeps_results(umtlib):
