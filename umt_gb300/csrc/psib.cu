@@ -357,6 +357,26 @@ int ensure_src_order(Ctx &c) {
   return 0;
 }
 
+// A row-copy kernel at the device's highest priority.  With equal
+// priorities, a copy launched while a stage still has blocks waiting got SM
+// slots only as that stage's last wave drained, and the link sat idle.
+template <typename... KArgs, typename... Args>
+static int launch_copy(void (*kern)(KArgs...), int blocks, cudaStream_t st, Args... args) {
+  int least = 0, greatest = 0;
+  UMT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributePriority;
+  at[0].val.priority = greatest;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(std::max(blocks, 1));
+  cfg.blockDim = dim3(256);
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  UMT_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+  return 0;
+}
+
 // Inside the host-facing graph: fork the chunk copies onto the side stream,
 // in stage order (a source chunk before the PsiB chunk that begins at the
 // same stage), each followed by its event.
@@ -372,18 +392,18 @@ int enqueue_psib_chunks(Ctx &c) {
       const int n = c.srcChunkOff[ks + 1] - c.srcChunkOff[ks];
       const size_t m = (size_t)n * (c.G / 2);
       const int blocks = (int)std::min<size_t>((m + 255) / 256, PSIB_GATHER_BLOCKS);
-      k_rows_gather<true><<<std::max(blocks, 1), 256, 0, c.stream2>>>(c.srcOrder + c.srcChunkOff[ks], n, c.G,
-                                                                        c.srcIn, c.STotal, c.STotal32);
-      UMT_CUDA(cudaGetLastError());
+      const int rl = launch_copy(k_rows_gather<true>, blocks, c.stream2, (const int *)(c.srcOrder + c.srcChunkOff[ks]),
+                                 n, c.G, (double *const *)c.srcIn, c.STotal, c.STotal32);
+      if (rl) return rl;
       UMT_CUDA(cudaEventRecord(c.evSrc[ks], c.stream2));
       ++ks;
     } else {
       const int n = c.chunkOff[kp + 1] - c.chunkOff[kp];
       const size_t m = (size_t)n * (c.G / 2);
       const int blocks = (int)std::min<size_t>((m + 255) / 256, PSIB_GATHER_BLOCKS);
-      k_rows_gather<false><<<std::max(blocks, 1), 256, 0, c.stream2>>>(c.rowOrder + c.chunkOff[kp], n, c.G,
-                                                                         c.psibIn, nullptr, c.psiB32);
-      UMT_CUDA(cudaGetLastError());
+      const int rl = launch_copy(k_rows_gather<false>, blocks, c.stream2, (const int *)(c.rowOrder + c.chunkOff[kp]),
+                                 n, c.G, (double *const *)c.psibIn, (double *)nullptr, c.psiB32);
+      if (rl) return rl;
       UMT_CUDA(cudaEventRecord(c.evChunk[kp], c.stream2));
       ++kp;
     }
@@ -414,9 +434,9 @@ int enqueue_exit_chunks(Ctx &c, int s) {
     const int n = c.exitChunkOff[k + 1] - c.exitChunkOff[k];
     const size_t m = (size_t)n * (c.G / 2);
     const int blocks = (int)std::min<size_t>((m + 255) / 256, PSIB_GATHER_BLOCKS);
-    k_rows_out<<<std::max(blocks, 1), 256, 0, c.stream3>>>(c.exitOrder + c.exitChunkOff[k], n, c.G, c.psiB32,
-                                                           c.psibOut);
-    UMT_CUDA(cudaGetLastError());
+    const int rl = launch_copy(k_rows_out, blocks, c.stream3, (const int *)(c.exitOrder + c.exitChunkOff[k]), n,
+                               c.G, (const float *)c.psiB32, (double *const *)c.psibOut);
+    if (rl) return rl;
   }
   return 0;
 }

@@ -700,7 +700,10 @@ static int sweep_via_graph(Ctx &c, int precision) {
     cudaError_t e = cudaStreamEndCapture(c.stream, &gr);
     if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
     if (e != cudaSuccess) return set_error(-3, "graph capture: %s", cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&ex, gr, 0);
+    // the host-facing graph runs its nodes at their own priorities (the row
+    // copies above the stages)
+    e = cudaGraphInstantiate(&ex, gr, precision == 1 && c.wantExitsThrough && !c.homog32
+                                          ? cudaGraphInstantiateFlagUseNodePriority : 0);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) { ex = nullptr; return set_error(-3, "graph instantiate: %s", cudaGetErrorString(e)); }
   }
