@@ -110,6 +110,10 @@ __global__ void __launch_bounds__(256) k_rows_out(const int *rows, int n, int G,
 // thread instead: 64 blocks hold ~2 MB in flight (24 blocks, ~0.8 MB, reached
 // only ~110 GB/s of the link's ~210 under its loaded latency).
 constexpr int PSIB_GATHER_BLOCKS = 64;
+// The exit-row copies write to the link, posted, so fewer blocks keep up: a
+// call took 15.8 ms with 32 blocks, 16.2 with 64 (more stage blocks
+// displaced) and 17.9 with 16 (the copies fell behind the stages).
+constexpr int EXIT_OUT_BLOCKS = 32;
 
 template <bool SRC>
 __global__ void __launch_bounds__(256) k_rows_gather(const int *rows, int n, int G, double *const *src,
@@ -433,7 +437,7 @@ int enqueue_exit_chunks(Ctx &c, int s) {
     UMT_CUDA(cudaStreamWaitEvent(c.stream3, c.evExit[k], 0));
     const int n = c.exitChunkOff[k + 1] - c.exitChunkOff[k];
     const size_t m = (size_t)n * (c.G / 2);
-    const int blocks = (int)std::min<size_t>((m + 255) / 256, PSIB_GATHER_BLOCKS);
+    const int blocks = (int)std::min<size_t>((m + 255) / 256, EXIT_OUT_BLOCKS);
     const int rl = launch_copy(k_rows_out, blocks, c.stream3, (const int *)(c.exitOrder + c.exitChunkOff[k]), n,
                                c.G, (const float *)c.psiB32, (double *const *)c.psibOut);
     if (rl) return rl;
