@@ -233,85 +233,89 @@ static int alloc_word(double ***w, const char *what) {
   return 0;
 }
 
-// The exiting rows by the stage that writes them, in chunks of ~4 MB or
-// more, each copied out after the last stage that writes one of its rows.
-static int ensure_exit_order(Ctx &c) {
-  if (c.exitOrder) return 0;
+// The PsiB rows (a*nb + b) counting-sorted by stage: the rows the sweep
+// reads by the stage that reads them, the rows it reads nowhere last (stage
+// S); with EXIT, the exiting rows by the stage that writes them.  *order
+// (device) and start[s] = the first entry of stage s, start[S + 1] = total.
+template <bool EXIT>
+static int row_order(Ctx &c, const char *what, int **orderOut, std::vector<int> &start) {
   const int S = c.sch.nStages;
   int *count = nullptr, *order = nullptr;
-  if (cudaMalloc((void **)&count, (size_t)(S + 1) * sizeof(int)) != cudaSuccess)
-    return set_error(UMT_ERR_NOMEM, "exit row order: allocation failed");
   auto fail = [&](int rc) { cudaFree(count); if (order) cudaFree(order); return rc; };
+  if (cudaMalloc((void **)&count, (size_t)(S + 1) * sizeof(int)) != cudaSuccess) {
+    count = nullptr;
+    return fail(set_error(UMT_ERR_NOMEM, "%s: allocation failed", what));
+  }
   cudaMemset(count, 0, (size_t)(S + 1) * sizeof(int));
-  k_row_count<true><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count);
+  k_row_count<EXIT><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count);
   std::vector<int> h(S + 1);
   if (cudaMemcpy(h.data(), count, (size_t)(S + 1) * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return fail(set_error(UMT_ERR_CUDA, "exit row order: %s", cudaGetErrorString(cudaGetLastError())));
-  std::vector<int> start(S + 2, 0);
+    return fail(set_error(UMT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(cudaGetLastError())));
+  start.assign(S + 2, 0);
   for (int s = 0; s <= S; ++s) start[s + 1] = start[s] + h[s];
-  if (start[S + 1] != start[S]) return fail(set_error(UMT_ERR_STATE, "exit row order: a row past the last stage"));
-  if (cudaMalloc((void **)&order, (size_t)std::max(start[S], 1) * sizeof(int)) != cudaSuccess) {
+  if (EXIT && start[S + 1] != start[S]) return fail(set_error(UMT_ERR_STATE, "%s: a row past the last stage", what));
+  if (cudaMalloc((void **)&order, (size_t)std::max(start[S + 1], 1) * sizeof(int)) != cudaSuccess) {
     order = nullptr;
-    return fail(set_error(UMT_ERR_NOMEM, "exit row order: allocation failed"));
+    return fail(set_error(UMT_ERR_NOMEM, "%s: allocation failed", what));
   }
   cudaMemcpy(count, start.data(), (size_t)(S + 1) * sizeof(int), cudaMemcpyHostToDevice);
-  k_row_scatter<true><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count,
+  k_row_scatter<EXIT><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count,
                                      order);
   const cudaError_t e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) return fail(set_error(UMT_ERR_CUDA, "exit row order: %s", cudaGetErrorString(e)));
-  std::vector<int> firstStage;
-  stage_chunks(start, S, false, c.G, c.exitChunkOff, firstStage, &c.exitChunkLast);
-  if (!c.stream3 && cudaStreamCreateWithFlags(&c.stream3, cudaStreamNonBlocking) != cudaSuccess) {
-    c.stream3 = nullptr;
-    return fail(set_error(UMT_ERR_CUDA, "exit row order: stream creation failed"));
-  }
-  if (!c.evExitJoin && cudaEventCreateWithFlags(&c.evExitJoin, cudaEventDisableTiming) != cudaSuccess) {
-    c.evExitJoin = nullptr;
-    return fail(set_error(UMT_ERR_CUDA, "exit row order: event creation failed"));
-  }
-  const int re = ensure_events(c.evExit, c.exitChunkLast.size());
-  if (re) return fail(re);
+  if (e != cudaSuccess) return fail(set_error(UMT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e)));
   cudaFree(count);
-  c.exitOrder = order;                             // kept only once its chunks, stream and events exist
+  *orderOut = order;
   return 0;
 }
 
+// The exiting rows by the stage that writes them, in chunks of ~4 MB or
+// more, each copied out after the last stage that writes one of its rows.
+// Kept (c.exitOrder) only once its chunks, stream and events exist.
+static int ensure_exit_order(Ctx &c) {
+  if (c.exitOrder) return 0;
+  int *order = nullptr;
+  std::vector<int> start, firstStage;
+  int rc = row_order<true>(c, "exit row order", &order, start);
+  if (rc) return rc;
+  stage_chunks(start, c.sch.nStages, false, c.G, c.exitChunkOff, firstStage, &c.exitChunkLast);
+  if (!c.stream3 && cudaStreamCreateWithFlags(&c.stream3, cudaStreamNonBlocking) != cudaSuccess) {
+    c.stream3 = nullptr;
+    rc = set_error(UMT_ERR_CUDA, "exit row order: stream creation failed");
+  }
+  if (!rc && !c.evExitJoin && cudaEventCreateWithFlags(&c.evExitJoin, cudaEventDisableTiming) != cudaSuccess) {
+    c.evExitJoin = nullptr;
+    rc = set_error(UMT_ERR_CUDA, "exit row order: event creation failed");
+  }
+  if (!rc) rc = ensure_events(c.evExit, c.exitChunkLast.size());
+  if (rc) {
+    cudaFree(order);
+    return rc;
+  }
+  c.exitOrder = order;
+  return 0;
+}
+
+// The rows the sweep reads, in chunks of ~4 MB or more in stage order, then
+// the rows no stage reads; then the exit rows.  Kept (c.rowOrder) only once
+// its chunks and their events exist.
 int ensure_psib_order(Ctx &c) {
   if (c.rowOrder) return ensure_exit_order(c);
   if (!c.afp32 || !c.psiB32) return set_error(UMT_ERR_STATE, "FP32 flux not allocated");
   if ((long long)c.A * c.nb >= (1LL << 31)) return set_error(UMT_ERR_ARG, "PsiB rows exceed 2^31");
   int rc = ensure_bface(c);
   if (rc) return rc;
-  const int S = c.sch.nStages;
-  int *count = nullptr, *order = nullptr;
-  if (cudaMalloc((void **)&count, (size_t)(S + 1) * sizeof(int)) != cudaSuccess)
-    return set_error(UMT_ERR_NOMEM, "PsiB row order: allocation failed");
-  // the order is kept (c.rowOrder) only once it, its chunks and their events exist
-  auto fail = [&](int rc_) { cudaFree(count); if (order) cudaFree(order); return rc_; };
-  cudaMemset(count, 0, (size_t)(S + 1) * sizeof(int));
-  k_row_count<false><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count);
-  std::vector<int> h(S + 1);
-  if (cudaMemcpy(h.data(), count, (size_t)(S + 1) * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return fail(set_error(UMT_ERR_CUDA, "PsiB row order: %s", cudaGetErrorString(cudaGetLastError())));
-  std::vector<int> start(S + 2, 0);
-  for (int s = 0; s <= S; ++s) start[s + 1] = start[s] + h[s];
-  const int total = start[S + 1];
-  if (cudaMalloc((void **)&order, (size_t)std::max(total, 1) * sizeof(int)) != cudaSuccess) {
-    order = nullptr;
-    return fail(set_error(UMT_ERR_NOMEM, "PsiB row order: allocation failed"));
+  int *order = nullptr;
+  std::vector<int> start;
+  rc = row_order<false>(c, "PsiB row order", &order, start);
+  if (rc) return rc;
+  stage_chunks(start, c.sch.nStages, true, c.G, c.chunkOff, c.chunkStage);
+  rc = ensure_side_stream(c);
+  if (!rc) rc = ensure_events(c.evChunk, c.chunkStage.size());
+  if (!rc) rc = alloc_word(&c.psibIn, "PsiB source word");
+  if (rc) {
+    cudaFree(order);
+    return rc;
   }
-  cudaMemcpy(count, start.data(), (size_t)(S + 1) * sizeof(int), cudaMemcpyHostToDevice);
-  k_row_scatter<false><<<1024, 256>>>(c.A, c.nb, c.nc, c.nz, S, c.bFace, c.afp32, c.cToZone, c.sch.level, count,
-                                      order);
-  const cudaError_t e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) return fail(set_error(UMT_ERR_CUDA, "PsiB row order: %s", cudaGetErrorString(e)));
-  // chunks of ~4 MB or more in stage order, then the rows no stage reads
-  stage_chunks(start, S, true, c.G, c.chunkOff, c.chunkStage);
-  int re = ensure_side_stream(c);
-  if (!re) re = ensure_events(c.evChunk, c.chunkStage.size());
-  if (!re) re = alloc_word(&c.psibIn, "PsiB source word");
-  if (re) return fail(re);
-  cudaFree(count);
   c.rowOrder = order;
   return ensure_exit_order(c);
 }
