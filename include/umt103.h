@@ -159,6 +159,11 @@ int umt103_get_psi(double *Psi, double *PsiB, int precision);
  * exiting boundary fluxes written into PsiB; with savePsi the new angular
  * flux becomes Psi.  STotal may be NULL (zero source, the mini-app case);
  * PhiTotal_out and PsiB_inout may be NULL (results stay on the device).
+ * With UMT_FP32 only the PsiB rows the sweep reads are read and only the
+ * rows it writes are written; the others keep their values bit for bit.
+ * Host arrays in page-locked memory (16-byte aligned) are read and written
+ * in place while the stages run; pageable ones are copied whole before and
+ * after.  The results are the same either way.
  */
 int umt103_sweep(const double *STotal, int savePsi, double *PhiTotal_out,
                  double *PsiB_inout, int precision);
